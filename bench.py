@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark of the batched adaptive-precision point rasterizer on GB300.
+
+Workload (default): 1,000,000,000 synthetic terrain points over 10 x 10 km in
+the LAS-derived batched layout, one 1920x1080 view from the reference's
+zoom-to-cloud pose (src/main.cpp:251-270).  One step = one frame: cull +
+raster + resolve (+ re-clear), the dispatch sequence of
+compute_loop_las.h:117-304.  `value` is Gpoints/s with the cloud resident in
+HBM; `e2e` is the same frame through the C ABI with the layout copied from
+pinned host buffers and the RGBA8 image copied back every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(name="terrain_1b_1080p", points=1_000_000_000, extent=10_000.0, seed=1,
+                width=1920, height=1080)
+CPU_SAMPLE_POINTS = 32_000_000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--points", type=int, default=WORKLOAD["points"])
+    ap.add_argument("--payload", default="color", choices=["color", "index"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def camera(box_min, box_max, width, height):
+    from compute_rasterizer_gb300 import synth
+    yaw, pitch, radius, target = synth.zoom_to_cloud(box_min, box_max)
+    view = synth.orbit_view(yaw, pitch, radius, target)
+    proj = synth.perspective(60.0, width / height, 0.1, 200000.0)
+    return view, proj
+
+
+class Clocks:
+    """nvidia-smi samples (SM clock, throttle reasons) while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.1)
+        self.p.terminate()
+        self.p.wait()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_sample(points_full: int, extent_full: float, seed: int, sample: int):
+    """A bounded sample of the workload for the CPU: the corner of the same
+    terrain (same seed, noise wavelength and point density), Morton-sorted and
+    encoded on the host, viewed by the full cloud's camera."""
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import synth
+    ext = extent_full * (sample / points_full) ** 0.5
+    p = synth.synth_params(L.SYNTH_TERRAIN, ext, seed, wavelength=extent_full / 4.0)
+    rec, hdr = synth.las_records_host(p, sample)
+    enc = encode_parallel(rec, sample, hdr)
+    return p, hdr, enc, ext
+
+
+def encode_parallel(rec, n, hdr, threads=None):
+    """cr_encode_las over batch-aligned chunks on host threads (ctypes drops the GIL)."""
+    import concurrent.futures as cf
+
+    from compute_rasterizer_gb300 import _lib as L
+    lib = L.load()
+    nb = int(lib.cr_num_batches(n))
+    batches = np.zeros(nb, L.BATCH_DTYPE)
+    st = [np.zeros(n, np.uint32) for _ in range(4)]
+    sc, of, mn = (np.ascontiguousarray(x[:], np.float64) for x in (hdr.scale, hdr.offset, hdr.min))
+    threads = threads or os.cpu_count() or 1
+    per = max(1, -(-nb // threads))
+
+    def job(k):
+        b0, b1 = k * per, min(nb, (k + 1) * per)
+        if b0 >= b1:
+            return 0
+        p0, p1 = b0 * 10240, min(n, b1 * 10240)
+        return lib.cr_encode_las(rec.ctypes.data + p0 * 26, p1 - p0, 26, 2, sc.ctypes.data,
+                                 of.ctypes.data, mn.ctypes.data, p0, 0,
+                                 batches.ctypes.data + b0 * 64,
+                                 *(s.ctypes.data + p0 * 4 for s in st))
+    with cf.ThreadPoolExecutor(threads) as ex:
+        assert all(r == 0 for r in ex.map(job, range(threads)))
+    return (batches, *st)
+
+
+def time_oracle(frame, enc, n, threads, min_seconds=0.0, steps=1, warmup=0):
+    from oracle import oracle as O
+    batches, lo, md, hi, rgba = enc
+    lo, md, hi, rgba = (O.pad_stream(x) for x in (lo, md, hi, rgba))
+    fb = np.empty(O.fb_words(frame.width, frame.height), np.uint64)
+    lib = O.lib()
+    b = np.ascontiguousarray(batches)
+
+    def one():
+        fb.fill(0xFF800000FF800000)
+        lib.or_raster_batched_mt(C.byref(frame), b.ctypes.data, len(b), n, lo.ctypes.data,
+                                 md.ctypes.data, hi.ctypes.data, rgba.ctypes.data, fb.ctypes.data,
+                                 threads)
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    frames = 0
+    while frames < steps or time.perf_counter() - t0 < min_seconds:
+        one()
+        frames += 1
+    dt = time.perf_counter() - t0
+    return dt / frames, frames
+
+
+def reference_arm(args, world, rank):
+    """--impl reference: the oracle (the reference's CPU restatement) on the host cores."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    n_full = args.points
+    s = min(CPU_SAMPLE_POINTS, n_full)
+    p, hdr, enc, ext = cpu_sample(n_full, WORKLOAD["extent"], WORKLOAD["seed"], s)
+    full_max = np.array([WORKLOAD["extent"], WORKLOAD["extent"], hdr.max[2]])
+    view, proj = camera(np.array(hdr.min[:]), full_max, WORKLOAD["width"], WORKLOAD["height"])
+    payload = O.PAYLOAD_COLOR if args.payload == "color" else O.PAYLOAD_INDEX
+    fr = O.make_frame(view, proj, WORKLOAD["width"], WORKLOAD["height"], np.array(hdr.min[:])[None],
+                      1, O.L0_X12, payload)
+    cores = os.cpu_count() or 1
+    per_frame, frames = time_oracle(fr, enc, s, cores, steps=args.steps, warmup=min(args.warmup, 3))
+    v = s / per_frame / 1e9
+    sample = (f"{s:,} points: the {ext:.0f} m corner of the same 10 km terrain at the same density, "
+              f"same camera; oracle {args.steps} frames")
+    out = {"impl": "reference", "metric": metric_name(), "value": round(v, 4),
+           "unit": "Gpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(per_frame * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic",
+           "config": config_dict(args),
+           "cpu_baseline": {"value": round(v, 4), "unit": "Gpoints/s", "cores": cores,
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": round(v, 4), "unit": "Gpoints/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def metric_name():
+    return "Gpoints/s at 1B points (frame = cull + raster + resolve)"
+
+
+def config_dict(args):
+    return {"workload": WORKLOAD["name"], "points": args.points, "extent_m": WORKLOAD["extent"],
+            "width": WORKLOAD["width"], "height": WORKLOAD["height"], "method": "loop_las",
+            "payload": args.payload, "view": "zoom-to-cloud orbit pose (yaw 0.53, pitch -0.68)",
+            "l2": "no flush: inputs (8-16 GB) exceed the 129 MB L2",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    import torch
+
+    import compute_rasterizer_gb300 as cr
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import synth
+
+    torch.cuda.set_device(local)
+    ctx = cr.Context(local)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    n = args.points
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    sp = synth.synth_params(L.SYNTH_TERRAIN, WORKLOAD["extent"], WORKLOAD["seed"] + rank)
+    cloud, hdr = synth.build_cloud_device(ctx, sp, n, sh)
+    bmin, bmax = np.array(hdr.min[:]), np.array(hdr.max[:])
+    view, proj = camera(bmin, bmax, W, H)
+    cv = cr.make_view(view, proj, W, H)
+    payload = L.PAYLOAD_COLOR if args.payload == "color" else L.PAYLOAD_INDEX
+    params = cr.default_params(L.METHOD_LOOP_LAS, payload=payload)
+    fb = ctx.framebuffer(W, H)
+    fb.clear(stream=sh)
+
+    def frames(k):
+        for _ in range(k):
+            ctx.render(cloud, cv, params, fb, sh)
+
+    frames(max(3, args.warmup))
+    ctx.sync(sh)
+    stats = ctx.frame_stats(cloud, params)
+    clocks = Clocks(local)
+    frames(20)  # keep the GPU loaded while the sampler starts
+    ctx.timing_enable(args.steps)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    frames(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+        dist.barrier()
+    ctx.sync(sh)
+    raster_ms = ctx.timing_read(L.STAGE_RASTER, args.steps)
+    cull_ms = ctx.timing_read(L.STAGE_CULL, args.steps)
+    resolve_ms = ctx.timing_read(L.STAGE_RESOLVE, args.steps)
+    ctx.timing_enable(0)
+    frame_s = elapsed / args.steps
+    value = world * n / frame_s / 1e9
+    peak, peak_kind = measured_peaks()
+    raster_s = float(np.mean(raster_ms)) / 1e3
+    achieved = stats.stream_bytes / raster_s / 1e9
+    prof = ROOT / "profiles" / "raster_terrain_1b_traffic.json"
+    traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch") if prof.exists() else None
+
+    out = {"metric": metric_name(), "value": round(value, 3), "unit": "Gpoints/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(frame_s * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic",
+           "config": config_dict(args),
+           "roofline": {"bound": "hbm", "kernel": "k_batched (raster)",
+                        "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                        "traffic": traffic,
+                        "algorithmic_bytes_per_launch": int(stats.stream_bytes),
+                        "raster_ms": round(raster_s * 1e3, 4)},
+           "stages_ms": {"cull": round(float(np.mean(cull_ms)), 4),
+                         "raster": round(raster_s * 1e3, 4),
+                         "resolve": round(float(np.mean(resolve_ms)), 4)},
+           "frame_stats": {"batches_visible": int(stats.batches_visible),
+                           "batches_dispatched": int(stats.batches_dispatched),
+                           "points_per_level": list(stats.points_per_level)},
+           "gpu_launches": 3 * args.steps, "clocks": clk}
+
+    if not args.no_extras:
+        out["extras"] = extras(ctx, cloud, cv, fb, sh, n, args)
+    if not args.no_e2e:
+        out["e2e"] = e2e(ctx, cloud, cv, params, fb, sh, n, args, bmin)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args, view, proj)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def extras(ctx, cloud, cv, fb, sh, n, args):
+    """The same frame with the index payload (loop_las as registered) and HQS."""
+    import torch
+
+    import compute_rasterizer_gb300 as cr
+    from compute_rasterizer_gb300 import _lib as L
+    res = {}
+    k = max(5, min(args.steps, 50))
+    for name, method, payload, kind in (("index_payload", L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX, L.FB_U64),
+                                        ("hqs", L.METHOD_LOOP_LAS_HQS, L.PAYLOAD_INDEX, L.FB_HQS)):
+        f = ctx.framebuffer(fb.W, fb.H, kind)
+        f.clear(0xFF800000 if kind == L.FB_HQS else L.DEFAULT_CLEAR, stream=sh)
+        p = cr.default_params(method, payload=payload)
+        for _ in range(3):
+            ctx.render(cloud, cv, p, f, sh)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            ctx.render(cloud, cv, p, f, sh)
+        ctx.sync(sh)
+        dt = (time.perf_counter() - t0) / k
+        res[name] = {"ms_per_frame": round(dt * 1e3, 4), "gpoints_per_s": round(n / dt / 1e9, 3)}
+        f.close()
+    return res
+
+
+def e2e(ctx, cloud, cv, params, fb, sh, n, args, box_min):
+    """Frame through the C ABI from pinned host buffers: upload of the batch
+    records and all four streams, render, image download, every step."""
+    import torch
+
+    from compute_rasterizer_gb300 import _lib as L
+    lib = L.load()
+    host = {}
+    for which, key in ((0, "batches"), (L.STREAM_LOW, "low"), (L.STREAM_MED, "med"),
+                       (L.STREAM_HIG, "hig"), (L.STREAM_RGBA, "rgba")):
+        nbytes = cloud.nb * 64 if which == 0 else n * 4
+        t = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        ctx.check(lib.cr_cloud_read(ctx.handle, cloud.handle, which, t.data_ptr(), nbytes, sh), "read")
+        host[key] = t
+    img = torch.empty(fb.W * fb.H * 4, dtype=torch.uint8, pin_memory=True)
+    box = np.ascontiguousarray(box_min, np.float64)
+    ctx.sync(sh)
+
+    def step():
+        ctx.check(lib.cr_cloud_upload(ctx.handle, cloud.handle, host["batches"].data_ptr(),
+                                      host["low"].data_ptr(), host["med"].data_ptr(),
+                                      host["hig"].data_ptr(), host["rgba"].data_ptr(),
+                                      box.ctypes.data, sh), "upload")
+        ctx.render(cloud, cv, params, fb, sh)
+        ctx.check(lib.cr_fb_read(ctx.handle, fb.handle, L.FB_IMAGE, img.data_ptr(), img.numel(), sh),
+                  "image read")
+    step()
+    ctx.sync(sh)
+    k = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
+    ctx.sync(sh)
+    dt = (time.perf_counter() - t0) / k
+    h2d = cloud.nb * 64 + 4 * n * 4
+    return {"value": round(n / dt / 1e9, 4), "unit": "Gpoints/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": fb.W * fb.H * 4, "ms_per_step": round(dt * 1e3, 3),
+            "steps": k, "path": "cr_cloud_upload + cr_render + cr_fb_read (pinned host buffers)"}
+
+
+def cpu_baseline(args, view, proj):
+    """The oracle's multi-threaded raster on a bounded sample, on this host's cores."""
+    from oracle import oracle as O
+    s = min(CPU_SAMPLE_POINTS, args.points)
+    p, hdr, enc, ext = cpu_sample(args.points, WORKLOAD["extent"], WORKLOAD["seed"], s)
+    payload = O.PAYLOAD_COLOR if args.payload == "color" else O.PAYLOAD_INDEX
+    fr = O.make_frame(view, proj, WORKLOAD["width"], WORKLOAD["height"], np.array(hdr.min[:])[None],
+                      1, O.L0_X12, payload)
+    cores = os.cpu_count() or 1
+    per_frame, frames = time_oracle(fr, enc, s, cores, min_seconds=10.0, warmup=1)
+    return {"value": round(s / per_frame / 1e9, 4), "unit": "Gpoints/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{s:,} points (the {ext:.0f} m corner of the same terrain, same density and "
+                      f"camera), {frames} frames"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,90 @@
+// cr_internal.h -- definitions shared by the host library (cr_api.cpp) and the
+// CUDA kernels (cr_kernels.cu, cr_synth.cu).  Not part of the C ABI.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/cr_raster.h"
+
+namespace cr {
+
+constexpr int kPointsPerBatch = CR_POINTS_PER_BATCH;
+constexpr int kInlineFiles = 8;       // per-file records passed in kernel parameters
+constexpr uint32_t kBackground = 0x00443322u;  // resolve.cs:141
+constexpr uint64_t kDefaultClear = 0xFF800000FF800000ull;  // compute_loop_las.h:292-296
+constexpr uint64_t kPlainReclear = 0xffffffffff3c321eull;  // compute_2021_earlyz/resolve.cs:77
+constexpr uint32_t kHqsDepthClear = 0xFF800000u;           // compute_loop_las_hqs.h:336-340
+// Zeroed words allocated past N in every stream: covers the 128-bit loads of
+// a partial last batch and the one-past-the-end point of the inclusive bound.
+constexpr int64_t kStreamPad = 64;
+
+// Device error bits (ctx scratch word kErrWord).
+enum : uint32_t {
+    kErrBadBatch = 1u,   // record with num_points/first_point/file_index out of range
+    kErrBadCount = 2u,   // work list overflow
+};
+
+// Per-(view, file) uniforms, computed on the host from double matrices
+// (compute_loop_las.h:141-200 + render.cs:145-174): 56 floats.
+struct FileRec {
+    float T[16];       // transform = mat4(proj * view * translate(boxMin))
+    float planes[24];  // frustumPlanes(transformFrustum): (nx, ny, nz, c) x 6
+    float VW[16];      // uniforms.view * file.world (float product)
+};
+
+struct ViewParams {
+    float P[16];       // uniforms.proj
+    int32_t W, H;
+    int32_t nfiles;
+    int32_t culling;
+    FileRec files[kInlineFiles];
+};
+
+// Scratch words at the head of the ctx scratch buffer.
+enum : int {
+    kItemCount = 0,   // work items appended by the cull kernel
+    kCursor0 = 1,     // dynamic work cursor, raster / HQS depth pass
+    kCursor1 = 2,     // dynamic work cursor, HQS color pass
+    kCounterWords = 4,
+    kErrWord = 4,     // sticky device error bits (cleared by cr_ctx_check)
+    kScratchHead = 8  // item list starts here
+};
+
+enum Mode : int { kModeRaster = 0, kModeHqsDepth = 1, kModeHqsColor = 2 };
+
+struct BatchedLaunch {
+    const cr_batch* batches;
+    const uint32_t* lo;
+    const uint32_t* md;
+    const uint32_t* hi;
+    const uint32_t* rgba;
+    int64_t capacity;      // allocated words per stream (N + padding)
+    uint64_t* fb;          // u64 framebuffer (raster)
+    uint32_t* depth;       // HQS depth
+    uint64_t* accum;       // HQS accumulators
+    uint32_t* scratch;     // counters + item list
+    int32_t quirks;
+    int32_t payload;
+    int32_t mode;
+};
+
+// Host-callable launchers (cr_kernels.cu).
+int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb_dispatch,
+                int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream);
+int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
+                   void* stream);
+int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
+                 uint64_t* fb, int grid, void* stream);
+int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgba,
+                         int64_t rgba_words, uint32_t* image, int clear_after, uint64_t clear,
+                         void* stream);
+int launch_resolve_color(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
+                         uint64_t clear, void* stream);
+int launch_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
+                         uint64_t clear, void* stream);
+int launch_resolve_hqs(int32_t W, int32_t H, uint32_t* depth, uint64_t* accum, uint32_t* image,
+                       int clear_after, void* stream);
+int launch_fill_u64(uint64_t* p, int64_t n, uint64_t v, void* stream);
+int launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, void* stream);
+
+}  // namespace cr

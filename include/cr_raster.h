@@ -1,0 +1,245 @@
+/*
+ * cr_raster.h -- C ABI of the GB300 point-rasterizer hot path.
+ *
+ * This library replaces the render dispatches of the compute_rasterizer
+ * `Method` plugins (include/Method.h:10-24) for the LAS-derived batched layout
+ * ("loop_las", "loop_las_prefetch", "loop_las_hqs") and the plain 16-byte path
+ * ("(2021) early-z").  Every entry point takes plain pointers and sizes, returns
+ * a cr_status and never aborts; a failed call leaves a message that
+ * cr_last_error() returns.  Device work is enqueued on the caller's CUDA stream
+ * (`stream` arguments are cudaStream_t values passed as void*; NULL = legacy
+ * default stream).
+ *
+ * Data layout (one GPU, device resident):
+ *   batches   cr_batch[B]            64 B records, one per <= 10,240 points
+ *   xyz_low   uint32[N]  10-bit x|y<<10|z<<20, bits 29..20 of the 30-bit coords
+ *   xyz_med   uint32[N]  bits 19..10          (needed by levels 0-1)
+ *   xyz_hig   uint32[N]  bits  9..0           (needed by level 0)
+ *   rgba      uint32[N]  R | G<<8 | B<<16
+ *   fb        uint64[W*H + W + 1]   depth-bits<<32 | payload, plus a guard tail
+ * Streams are allocated with zeroed padding past N so that vector loads of a
+ * partial last batch stay in bounds.
+ */
+#ifndef CR_RASTER_H
+#define CR_RASTER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CR_ABI_VERSION 1
+#define CR_POINTS_PER_BATCH 10240 /* Resources.h:4-6: POINTS_PER_THREAD 80 x WORKGROUP_SIZE 128 */
+#define CR_MAX_POINTS_PER_LOAD 1024000 /* Resources.h:8 MAX_POINTS_PER_BATCH */
+
+typedef enum cr_status {
+    CR_OK = 0,
+    CR_ERR_INVALID_ARG = 1,
+    CR_ERR_OUT_OF_MEMORY = 2,
+    CR_ERR_ADMISSION_REJECTED = 3,
+    CR_ERR_TIMEOUT = 4,
+    CR_ERR_CUDA = 5,
+    CR_ERR_DEVICE_FLAG = 6, /* a kernel found an out-of-range record and skipped it */
+    CR_ERR_UNSUPPORTED = 7,
+    CR_ERR_NOT_FOUND = 8
+} cr_status;
+
+/* Method ids; names as registered by the reference (compute_loop_las.h:82,
+ * compute_loop_las2.h:82, compute_loop_las_hqs.h:88, compute_2021_earlyz.h:52). */
+typedef enum cr_method {
+    CR_METHOD_LOOP_LAS = 0,          /* "loop_las" */
+    CR_METHOD_LOOP_LAS_PREFETCH = 1, /* "loop_las_prefetch" */
+    CR_METHOD_LOOP_LAS_HQS = 2,      /* "loop_las_hqs" */
+    CR_METHOD_EARLYZ = 3             /* "(2021) early-z" */
+} cr_method;
+
+typedef enum cr_payload {
+    CR_PAYLOAD_INDEX = 0, /* low word = global point index; color gathered at resolve (render.cs:417) */
+    CR_PAYLOAD_COLOR = 1  /* low word = the point's RGBA8 word */
+} cr_payload;
+
+/* Reference behaviours kept for drop-in parity (each method's default set is
+ * what the reference does; pass 0 for the corrected behaviour). */
+typedef enum cr_quirk {
+    CR_QUIRK_L0_X12 = 1,            /* 30-bit decode takes Y, Z low bits from X (render.cs:352-353) */
+    CR_QUIRK_INCLUSIVE_END = 2,     /* `localIndex > numPoints` (las2/render.cs:341, hqs/depth.cs:276) */
+    CR_QUIRK_DISPATCH_BY_POINTS = 4 /* ceil(numPoints/10240) workgroups (compute_loop_las2.h:234) */
+} cr_quirk;
+
+#define CR_QUIRKS_METHOD_DEFAULT (-1)
+
+/* 64-byte batch record: render.cs:22-40, LasLoaderSparse.cpp:109-121. */
+typedef struct cr_batch {
+    int32_t state;
+    float min_x, min_y, min_z;
+    float max_x, max_y, max_z;
+    int32_t num_points;
+    int32_t first_point; /* global index of the batch's first point */
+    int32_t file_index;
+    int32_t padding[6];
+} cr_batch;
+
+/* Plain 16-byte point: compute_2021_earlyz/render.cs:15-20. */
+typedef struct cr_vertex {
+    float x, y, z;
+    uint32_t color;
+} cr_vertex;
+
+/* One view: Renderer.h:78-82 View{dmat4 view, proj} plus the framebuffer size.
+ * Matrices are column-major doubles, like glm::dmat4. */
+typedef struct cr_view {
+    double view[16];
+    double proj[16];
+    int32_t width, height;
+} cr_view;
+
+typedef struct cr_render_params {
+    int32_t method;          /* cr_method */
+    int32_t payload;         /* cr_payload (batched methods) */
+    int32_t quirks;          /* cr_quirk mask, or CR_QUIRKS_METHOD_DEFAULT */
+    int32_t frustum_culling; /* Debug::frustumCullingEnabled (Debug.h:16-29), default 1 */
+    int32_t resolve;         /* 1: resolve into the fb's RGBA8 image after rasterizing */
+    int32_t clear_after;     /* 1: re-clear the fb after the resolve (compute_loop_las.h:288-301) */
+    uint64_t clear_value;    /* fb clear word; default 0xFF800000FF800000 (-inf bits x2) */
+    int32_t block_threads;   /* threads per CTA for the batched kernels; 0 = tuned default */
+    int32_t ctas_per_sm;     /* persistent CTAs per SM; 0 = tuned default */
+    int32_t views_per_group; /* multi-view: views sharing one point fetch; 0 = tuned default */
+    int32_t reserved[5];
+} cr_render_params;
+
+typedef struct cr_ctx cr_ctx;
+typedef struct cr_cloud cr_cloud;
+typedef struct cr_fb cr_fb;
+
+/* ---- library ------------------------------------------------------------- */
+int32_t cr_abi_version(void);
+const char* cr_status_string(cr_status s);
+const char* cr_method_name(int32_t method);                 /* Method::name */
+const char* cr_method_group(int32_t method);                /* Method::group */
+const char* cr_method_description(int32_t method);          /* Method::description */
+cr_status cr_method_find(const char* name, int32_t* method); /* Runtime.h:43-49 by name */
+void cr_render_params_default(int32_t method, cr_render_params* out);
+
+/* ---- context (one per device; not thread-safe per handle) ---------------- */
+cr_status cr_ctx_create(int32_t device, cr_ctx** out);
+cr_status cr_ctx_destroy(cr_ctx* ctx);
+const char* cr_last_error(const cr_ctx* ctx);
+/* Waits for `stream`, then reports a device-side error flag raised since the
+ * last check (CR_ERR_DEVICE_FLAG) and clears it. */
+cr_status cr_ctx_check(cr_ctx* ctx, void* stream);
+int32_t cr_ctx_num_sms(const cr_ctx* ctx);
+
+/* ---- clouds: the LAS-derived layout (LasLoaderSparse.h:86-91) ------------ */
+enum { CR_STREAM_LOW = 1, CR_STREAM_MED = 2, CR_STREAM_HIG = 4, CR_STREAM_RGBA = 8, CR_STREAM_ALL = 15 };
+
+/* Allocates device storage for `num_points` points in `num_batches` records
+ * across `num_files` files (per-file boxMin feeds the world matrix). */
+cr_status cr_cloud_create(cr_ctx* ctx, int64_t num_points, int64_t num_batches, int32_t num_files,
+                          int32_t stream_mask, cr_cloud** out);
+/* Host -> device copies (pinned or pageable).  Any stream pointer may be NULL
+ * to leave that stream untouched.  Records are validated on the host:
+ * 0 <= num_points <= 10240, first_point + num_points <= N, file_index < files,
+ * finite AABB. */
+cr_status cr_cloud_upload(cr_ctx* ctx, cr_cloud* cloud, const cr_batch* batches,
+                          const uint32_t* xyz_low, const uint32_t* xyz_med,
+                          const uint32_t* xyz_hig, const uint32_t* rgba,
+                          const double* file_box_min /* [3 * num_files] */, void* stream);
+/* Device pointers of a cloud, for GPU-side writers (the GPU encoder). */
+cr_status cr_cloud_device(const cr_cloud* cloud, cr_batch** batches, uint32_t** xyz_low,
+                          uint32_t** xyz_med, uint32_t** xyz_hig, uint32_t** rgba);
+cr_status cr_cloud_set_files(cr_ctx* ctx, cr_cloud* cloud, const double* file_box_min);
+/* Device -> host copy of one array of the layout (CR_STREAM_LOW/MED/HIG/RGBA,
+ * or 0 for the batch records), enqueued on `stream` (caller syncs). */
+cr_status cr_cloud_read(cr_ctx* ctx, const cr_cloud* cloud, int32_t which, void* host_dst,
+                        int64_t bytes, void* stream);
+int64_t cr_cloud_num_points(const cr_cloud* cloud);
+int64_t cr_cloud_num_batches(const cr_cloud* cloud);
+cr_status cr_cloud_destroy(cr_ctx* ctx, cr_cloud* cloud);
+
+/* Plain 16 B/point clouds (LasLoaderStandard.h). */
+cr_status cr_cloud_create_plain(cr_ctx* ctx, int64_t num_points, cr_cloud** out);
+cr_status cr_cloud_upload_plain(cr_ctx* ctx, cr_cloud* cloud, const cr_vertex* vertices,
+                                void* stream);
+cr_status cr_cloud_device_plain(const cr_cloud* cloud, cr_vertex** vertices);
+
+/* ---- framebuffers --------------------------------------------------------- */
+enum { CR_FB_U64 = 0, CR_FB_HQS = 1 };
+enum { CR_FB_WORDS = 0, CR_FB_DEPTH = 1, CR_FB_ACCUM = 2, CR_FB_IMAGE = 3 };
+
+/* u64: W*H + W + 1 words + RGBA8 image (u32 per pixel).
+ * HQS: u32 depth [W*H + W + 1], u64 accumulators [2 * (W*H + W + 1)], image. */
+cr_status cr_fb_create(cr_ctx* ctx, int32_t width, int32_t height, int32_t kind, cr_fb** out);
+cr_status cr_fb_destroy(cr_ctx* ctx, cr_fb* fb);
+/* u64 kind: every word = value.  HQS: depth = low 32 bits of value, accum = 0. */
+cr_status cr_fb_clear(cr_ctx* ctx, cr_fb* fb, uint64_t value, void* stream);
+/* Size in bytes of one of the fb's buffers (CR_FB_WORDS/DEPTH/ACCUM/IMAGE). */
+int64_t cr_fb_bytes(const cr_fb* fb, int32_t what);
+/* Device -> host copy of one buffer, enqueued on `stream` (caller syncs). */
+cr_status cr_fb_read(cr_ctx* ctx, const cr_fb* fb, int32_t what, void* host_dst, int64_t bytes,
+                     void* stream);
+cr_status cr_fb_device(const cr_fb* fb, int32_t what, void** device_ptr);
+
+/* ---- rendering: Method::render (compute_loop_las.h:117-304 and siblings) --
+ * Rasterizes `cloud` for `view` into `fb`; with params->resolve, resolves the
+ * image; with params->clear_after, re-clears the fb for the next frame.  A new
+ * fb must be cleared once with cr_fb_clear before its first frame. */
+cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
+                    const cr_render_params* params, cr_fb* fb, void* stream);
+
+/* Resolve only (resolve.cs); `cloud` supplies the color stream for the index
+ * payload and may be NULL otherwise. */
+cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params* params,
+                     cr_fb* fb, void* stream);
+
+/* ---- timer queries and frame counters --------------------------------------
+ * GLTimerQueries::timestamp pairs (src/GLTimerQueries.cpp:6-22) around the
+ * dispatches become CUDA events: while timing is on, every cr_render records
+ * an event at each stage boundary.  Stages: 0 cull, 1 raster (HQS: depth),
+ * 2 HQS color, 3 resolve. */
+enum { CR_STAGE_CULL = 0, CR_STAGE_RASTER = 1, CR_STAGE_HQS_COLOR = 2, CR_STAGE_RESOLVE = 3,
+       CR_NUM_STAGES = 4 };
+cr_status cr_timing_enable(cr_ctx* ctx, int32_t max_frames); /* 0 disables; resets */
+/* Synchronizes, then writes up to `max` per-frame milliseconds of `stage`
+ * (frames that did not run the stage report 0) and returns the frame count. */
+int32_t cr_timing_read(cr_ctx* ctx, int32_t stage, float* ms, int32_t max);
+
+/* Debug counters of the last cull (compute_loop_las.h:54-62 DebugData):
+ * visible batches and points per precision level and the bytes the raster
+ * reads for them.  Synchronizes. */
+typedef struct cr_frame_stats {
+    int64_t batches_dispatched;
+    int64_t batches_visible;
+    int64_t batches_per_level[5];
+    int64_t points_per_level[5];
+    int64_t stream_bytes;      /* coordinate words + color words (if read) + 64 B records */
+} cr_frame_stats;
+cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params* params,
+                              cr_frame_stats* out);
+
+/* ---- host-side layout builders (LasLoaderSparse.cpp:37-212) --------------- */
+int64_t cr_num_batches(int64_t num_points);
+/* Encodes `n` LAS point records (raw bytes, `bytes_per_point` stride) of one
+ * load task into batch records and the four streams.  `sparse_offset` is the
+ * global index of the first record (LasFile::sparse_point_offset + firstPoint). */
+cr_status cr_encode_las(const uint8_t* records, int64_t n, int32_t bytes_per_point,
+                        int32_t point_format, const double scale[3], const double offset[3],
+                        const double box_min[3], int64_t sparse_offset, int32_t file_index,
+                        cr_batch* batches, uint32_t* xyz_low, uint32_t* xyz_med,
+                        uint32_t* xyz_hig, uint32_t* rgba);
+/* LasLoaderStandard.h:152-179: LAS records -> 16 B vertices. */
+cr_status cr_encode_standard(const uint8_t* records, int64_t n, int32_t bytes_per_point,
+                             int32_t point_format, const double scale[3], const double offset[3],
+                             const double box_min[3], cr_vertex* out);
+
+/* ---- host matrix setup (Camera.h:34-39, OrbitControls.h:116-135) ----------- */
+void cr_perspective(double fovy_deg, double aspect, double znear, double zfar, double out[16]);
+void cr_look_at(const double eye[3], const double center[3], const double up[3], double out[16]);
+void cr_orbit_view(double yaw, double pitch, double radius, const double target[3],
+                   double out_view[16]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

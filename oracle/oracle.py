@@ -1,0 +1,203 @@
+"""ctypes binding of the oracle (oracle.c): TEST INFRASTRUCTURE.
+
+Imported only by tests/, __graft_entry__.smoke() and the CPU-baseline leg of
+bench.py, always as the checker.  `build()` runs oracle/Makefile.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+GLMREF = HERE / "_ref" / "libglmref.so"
+
+L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS = 1, 2, 4
+PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
+
+
+class FileFrame(C.Structure):
+    _fields_ = [("transform", C.c_float * 16), ("planes", C.c_float * 24),
+                ("view_world", C.c_float * 16)]
+
+
+class Frame(C.Structure):
+    _fields_ = [("proj", C.c_float * 16), ("width", C.c_int32), ("height", C.c_int32),
+                ("frustum_culling", C.c_int32), ("quirks", C.c_int32), ("payload", C.c_int32),
+                ("num_files", C.c_int32), ("files", C.POINTER(FileFrame))]
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        _lib = C.CDLL(str(LIB))
+        P, I64, I32 = C.c_void_p, C.c_int64, C.c_int32
+        sig = {
+            "or_file_setup": [P, P, P, C.POINTER(FileFrame)],
+            "or_proj_float": [P, P],
+            "or_raster_batched": [C.POINTER(Frame), P, I64, I64, P, P, P, P, P],
+            "or_raster_batched_mt": [C.POINTER(Frame), P, I64, I64, P, P, P, P, P, C.c_int],
+            "or_resolve_index": [I32, I32, P, P, P],
+            "or_resolve_color": [I32, I32, P, P],
+            "or_hqs_depth": [C.POINTER(Frame), P, I64, I64, P, P, P, P],
+            "or_hqs_color": [C.POINTER(Frame), P, I64, I64, P, P, P, P, P, P],
+            "or_hqs_resolve": [I32, I32, P, P],
+            "or_plain_transform": [P, P, P],
+            "or_raster_plain": [P, I32, I32, P, I64, P],
+            "or_resolve_plain": [I32, I32, P, P, C.c_uint64],
+            "or_encode_las": [P, I64, I32, I32, P, P, P, I64, I32, P, P, P, P, P],
+            "or_encode_standard": [P, I64, I32, I32, P, P, P, P],
+            "or_precision_level": [C.POINTER(Frame), C.POINTER(FileFrame), P, P],
+            "or_intersects_frustum": [P, P, P],
+            "or_perspective": [C.c_double] * 4 + [P],
+            "or_look_at": [P, P, P, P],
+            "or_inverse": [P, P],
+            "or_orbit_world": [C.c_double] * 3 + [P, P],
+            "or_morton3": [C.c_uint32] * 3,
+            "or_fnv1a64": [P, I64],
+            "or_dispatch_batches": [I64, I64, I32],
+        }
+        for k, v in sig.items():
+            getattr(_lib, k).argtypes = v
+            getattr(_lib, k).restype = None
+        for k in ("or_precision_level", "or_intersects_frustum"):
+            getattr(_lib, k).restype = C.c_int
+        _lib.or_morton3.restype = C.c_uint64
+        _lib.or_fnv1a64.restype = C.c_uint64
+        _lib.or_dispatch_batches.restype = C.c_int64
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def glmref() -> C.CDLL:
+    """The glm probe built from the reference's vendored glm (oracle/_ref)."""
+    g = C.CDLL(str(GLMREF))
+    P, D, I = C.c_void_p, C.c_double, C.c_int
+    sig = {"glmref_camera": [D, I, I, D, D, P, P, P],
+           "glmref_orbit_world": [D, D, D, P, P],
+           "glmref_look_at": [P, P, P, P],
+           "glmref_inverse": [P, P],
+           "glmref_file_record": [P, P, P, P, P, P, P],
+           "glmref_plain_transform": [P, P, P]}
+    for k, v in sig.items():
+        getattr(g, k).argtypes = v
+        getattr(g, k).restype = None
+    return g
+
+
+def fnv(a: np.ndarray) -> int:
+    a = np.ascontiguousarray(a)
+    return int(lib().or_fnv1a64(_p(a), a.nbytes))
+
+
+def make_frame(view, proj, width, height, box_mins, culling=1, quirks=0, payload=0):
+    """Frame + per-file records from double matrices (compute_loop_las.h:141-200)."""
+    o = lib()
+    view = np.ascontiguousarray(view, np.float64).reshape(16)
+    proj = np.ascontiguousarray(proj, np.float64).reshape(16)
+    box_mins = np.ascontiguousarray(box_mins, np.float64).reshape(-1, 3)
+    files = (FileFrame * len(box_mins))()
+    for i, bm in enumerate(box_mins):
+        bm = np.ascontiguousarray(bm)
+        o.or_file_setup(_p(view), _p(proj), _p(bm), C.byref(files[i]))
+    fr = Frame()
+    o.or_proj_float(_p(proj), C.cast(fr.proj, C.c_void_p))
+    fr.width, fr.height = int(width), int(height)
+    fr.frustum_culling, fr.quirks, fr.payload = int(culling), int(quirks), int(payload)
+    fr.num_files = len(box_mins)
+    fr.files = files
+    fr._keep = files
+    return fr
+
+
+def fb_words(width, height) -> int:
+    return width * height + width + 1
+
+
+def pad_stream(a, pad=64) -> np.ndarray:
+    """A stream with zeroed words past N (the device streams carry the same)."""
+    out = np.zeros(len(a) + pad, dtype=np.uint32)
+    out[:len(a)] = a
+    return out
+
+
+def raster_batched(frame, batches, n, low, med, hig, rgba, clear=0xFF800000FF800000,
+                   threads=1) -> np.ndarray:
+    fb = np.full(fb_words(frame.width, frame.height), clear, dtype=np.uint64)
+    low, med, hig = pad_stream(low), pad_stream(med), pad_stream(hig)
+    rgba = pad_stream(rgba) if rgba is not None else None
+    b = np.ascontiguousarray(batches)
+    if threads > 1:
+        lib().or_raster_batched_mt(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig),
+                                   _p(rgba), _p(fb), threads)
+    else:
+        lib().or_raster_batched(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig),
+                                _p(rgba), _p(fb))
+    return fb
+
+
+def resolve_index(width, height, fb, rgba) -> np.ndarray:
+    out = np.empty(width * height, dtype=np.uint32)
+    r = pad_stream(rgba)
+    lib().or_resolve_index(width, height, _p(fb), _p(r), _p(out))
+    return out
+
+
+def resolve_color(width, height, fb) -> np.ndarray:
+    out = np.empty(width * height, dtype=np.uint32)
+    lib().or_resolve_color(width, height, _p(fb), _p(out))
+    return out
+
+
+def hqs(frame, batches, n, low, med, hig, rgba):
+    depth = np.full(fb_words(frame.width, frame.height), 0xFF800000, dtype=np.uint32)
+    accum = np.zeros(2 * fb_words(frame.width, frame.height), dtype=np.uint64)
+    low, med, hig, rgba = (pad_stream(x) for x in (low, med, hig, rgba))
+    b = np.ascontiguousarray(batches)
+    lib().or_hqs_depth(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig), _p(depth))
+    lib().or_hqs_color(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig), _p(rgba),
+                       _p(depth), _p(accum))
+    img = np.empty(frame.width * frame.height, dtype=np.uint32)
+    lib().or_hqs_resolve(frame.width, frame.height, _p(accum), _p(img))
+    return depth, accum, img
+
+
+def plain(view, proj, width, height, vertices, clear=0xFFFFFFFFFFFFFFFF,
+          reclear=0xFFFFFFFFFF3C321E):
+    T = np.empty(16, np.float32)
+    view = np.ascontiguousarray(view, np.float64).reshape(16)
+    proj = np.ascontiguousarray(proj, np.float64).reshape(16)
+    lib().or_plain_transform(_p(view), _p(proj), _p(T))
+    fb = np.full(fb_words(width, height), clear, dtype=np.uint64)
+    v = np.ascontiguousarray(vertices)
+    lib().or_raster_plain(_p(T), width, height, _p(v), len(v), _p(fb))
+    fb_before = fb.copy()
+    img = np.empty(width * height, dtype=np.uint32)
+    lib().or_resolve_plain(width, height, _p(fb), _p(img), reclear)
+    return fb_before, img, fb
+
+
+def encode_las(records, n, bpp, fmt, scale, offset, box_min, sparse_offset=0, file_index=0):
+    nb = (n + 10239) // 10240
+    from compute_rasterizer_gb300._lib import BATCH_DTYPE
+    batches = np.zeros(nb, dtype=BATCH_DTYPE)
+    streams = [np.zeros(n, dtype=np.uint32) for _ in range(4)]
+    sc, of, bm = (np.ascontiguousarray(x, np.float64) for x in (scale, offset, box_min))
+    lib().or_encode_las(_p(records), n, bpp, fmt, _p(sc), _p(of), _p(bm), sparse_offset,
+                        file_index, _p(batches), *(_p(s) for s in streams))
+    return (batches, *streams)

@@ -1,0 +1,103 @@
+"""Shared test workloads: small seeded clouds, cameras, and GPU-vs-oracle runs."""
+from __future__ import annotations
+
+import numpy as np
+
+from compute_rasterizer_gb300 import _lib as L
+from compute_rasterizer_gb300 import default_params, make_view, synth
+from oracle import oracle as O
+
+QUIRKS = {L.METHOD_LOOP_LAS: O.L0_X12,
+          L.METHOD_LOOP_LAS_PREFETCH: O.INCLUSIVE_END | O.DISPATCH_BY_POINTS,
+          L.METHOD_LOOP_LAS_HQS: O.L0_X12 | O.INCLUSIVE_END | O.DISPATCH_BY_POINTS}
+
+
+def terrain_las(n=62674, extent=200.0, seed=7, kind=L.SYNTH_TERRAIN, **kw):
+    p = synth.synth_params(kind, extent, seed, **kw)
+    rec, hdr = synth.las_records_host(p, n)
+    return p, rec, hdr
+
+
+def encoded(n=62674, extent=200.0, seed=7, **kw):
+    p, rec, hdr = terrain_las(n, extent, seed, **kw)
+    batches, lo, md, hi, rgba = synth.encode_las(rec, n, hdr)
+    return dict(n=n, hdr=hdr, rec=rec, batches=batches, lo=lo, md=md, hi=hi, rgba=rgba,
+                box_min=synth.header_min(hdr), box_max=synth.header_max(hdr))
+
+
+def cameras(cl, width=320, height=240):
+    """Far (levels 2-4), near (levels 0-1) and partly-outside views of a cloud."""
+    views = camera_views(cl["box_min"], cl["box_max"], cl["batches"])
+    proj = synth.perspective(60.0, width / height, 0.1, 200000.0)
+    return {k: (v, proj, width, height) for k, v in views.items()}
+
+
+def camera_views(bmin, bmax, batches):
+    """far: the reference's zoom-to-cloud pose (levels 2-4); near: 1.5 m from a
+    batch centre (30-bit for that batch, 20-bit around it); mid: 30 m above the
+    same batch (20-bit); corner: partly outside the cloud (culling)."""
+    yaw, pitch, radius, target = synth.zoom_to_cloud(bmin, bmax)
+    size = bmax - bmin
+    b = batches[len(batches) // 2]
+    centre = bmin + 0.5 * np.array([b["min_x"] + b["max_x"], b["min_y"] + b["max_y"],
+                                    b["min_z"] + b["max_z"]], np.float64)
+    return {
+        "far": synth.orbit_view(yaw, pitch, radius, target),
+        "near": synth.orbit_view(0.3, -0.35, 1.5, centre),
+        "mid": synth.orbit_view(1.1, -1.2, 30.0, centre),
+        "corner": synth.orbit_view(2.0, -0.5, 0.3 * float(np.linalg.norm(size)), bmin + 0.1 * size),
+    }
+
+
+def oracle_frame(cam, box_mins, quirks, payload=O.PAYLOAD_INDEX, culling=1):
+    view, proj, w, h = cam
+    return O.make_frame(view, proj, w, h, box_mins, culling=culling, quirks=quirks,
+                        payload=payload)
+
+
+def gpu_raw(ctx, cloud, cam, method, payload=L.PAYLOAD_INDEX, quirks=L.QUIRKS_METHOD_DEFAULT,
+            culling=1, fb_kind=None, clear=L.DEFAULT_CLEAR, **kw):
+    """Rasterize only (no resolve); returns the Framebuffer."""
+    view, proj, w, h = cam
+    kind = fb_kind if fb_kind is not None else (
+        L.FB_HQS if method == L.METHOD_LOOP_LAS_HQS else L.FB_U64)
+    fb = ctx.framebuffer(w, h, kind)
+    fb.clear(0xFF800000 if kind == L.FB_HQS else clear)
+    params = default_params(method, payload=payload, quirks=quirks, frustum_culling=culling,
+                            resolve=0, clear_after=0, **kw)
+    ctx.render(cloud, make_view(view, proj, w, h), params, fb)
+    ctx.sync()
+    return fb, params
+
+
+def first_diff(a, b, n=5):
+    idx = np.nonzero(a != b)[0][:n]
+    return [(int(i), hex(int(a[i])), hex(int(b[i]))) for i in idx]
+
+
+IDENTITY = np.eye(4).reshape(16)
+
+
+def handmade_cloud(points, colors, box_min=(-1.0, -1.0, 0.0), box_max=(1.0, 1.0, 1.0),
+                   first_point=0, pad_before=0):
+    """One batch whose 10-bit words are given directly: points are integer
+    (X, Y, Z) in [0, 1023]; the decoded position is box_min + X * size / 1024.
+    With identity view and projection, NDC = decoded position and w = 1."""
+    pts = np.asarray(points, np.uint32).reshape(-1, 3)
+    n = pad_before + len(pts)
+    lo = np.zeros(n, np.uint32)
+    lo[pad_before:] = pts[:, 0] | (pts[:, 1] << 10) | (pts[:, 2] << 20)
+    rgba = np.zeros(n, np.uint32)
+    rgba[pad_before:] = np.asarray(colors, np.uint32)
+    b = np.zeros(1, L.BATCH_DTYPE)
+    b["min_x"], b["min_y"], b["min_z"] = box_min
+    b["max_x"], b["max_y"], b["max_z"] = box_max
+    b["num_points"] = len(pts)
+    b["first_point"] = pad_before
+    zeros = np.zeros(n, np.uint32)
+    return dict(n=n, batches=b, lo=lo, md=zeros.copy(), hi=zeros.copy(), rgba=rgba,
+                box_min=np.zeros(3), box_max=np.ones(3))
+
+
+def identity_cam(w=64, h=32):
+    return (IDENTITY, IDENTITY, w, h)

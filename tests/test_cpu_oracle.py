@@ -1,0 +1,202 @@
+"""CPU tests: the oracle pinned to the reference's glm matrix code, the product's
+host builders checked against the oracle, quirk semantics, and golden vectors."""
+import ctypes as C
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from compute_rasterizer_gb300 import _lib as L
+from compute_rasterizer_gb300 import synth
+from helpers import QUIRKS, cameras, encoded, handmade_cloud, identity_cam, oracle_frame
+from oracle import oracle as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "golden.json"
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def test_unorm_roundtrip_exact():
+    c = np.arange(256, dtype=np.float32)
+    r = (np.float32(255.0) * (c / np.float32(255.0))).astype(np.float32)
+    assert np.array_equal(r.astype(np.uint32), np.arange(256))
+
+
+@pytest.mark.skipif(not O.GLMREF.exists(), reason="reference glm probe not built (no reference tree)")
+def test_matrices_match_reference_glm():
+    g = O.glmref()
+    o = O.lib()
+    lib = L.load()
+    rng = np.random.default_rng(3)
+    for _ in range(300):
+        yaw, pitch = rng.uniform(-3, 3), rng.uniform(-1.5, 1.5)
+        radius = rng.uniform(10, 20000)
+        tgt = np.ascontiguousarray(rng.uniform(-1e4, 1e4, 3))
+        W, H = int(rng.integers(64, 4000)), int(rng.integers(64, 4000))
+        wg = np.zeros(16)
+        g.glmref_orbit_world(yaw, pitch, radius, _p(tgt), _p(wg))
+        wo = np.zeros(16)
+        o.or_orbit_world(yaw, pitch, radius, _p(tgt), _p(wo))
+        assert np.array_equal(wg, wo)
+        vg, pg = np.zeros(16), np.zeros(16)
+        g.glmref_camera(60.0, W, H, 0.1, 200000.0, _p(wg), _p(vg), _p(pg))
+        po = np.zeros(16)
+        o.or_perspective(math.pi * 60.0 / 180.0, W / H, 0.1, 200000.0, _p(po))
+        assert np.array_equal(po, pg)
+        # product host code: perspective + orbit view
+        pp = synth.perspective(60.0, W / H, 0.1, 200000.0)
+        assert np.array_equal(pp, pg)
+        vp = synth.orbit_view(yaw, pitch, radius, tgt)
+        assert np.array_equal(vp.astype(np.float32), vg.astype(np.float32))
+        # per-file float uniforms (compute_loop_las.h:166-200)
+        bm = np.ascontiguousarray(rng.uniform(-1e5, 1e5, 3))
+        tf, wf, vwf, pf = (np.zeros(16, np.float32) for _ in range(4))
+        g.glmref_file_record(_p(vg), _p(pg), _p(bm), _p(tf), _p(wf), _p(vwf), _p(pf))
+        ff = O.FileFrame()
+        o.or_file_setup(_p(vg), _p(pg), _p(bm), C.byref(ff))
+        assert np.array_equal(np.frombuffer(ff.transform, np.float32), tf)
+        assert np.array_equal(np.frombuffer(ff.view_world, np.float32), vwf)
+        a, b = np.zeros(16, np.float32), np.zeros(16, np.float32)
+        g.glmref_plain_transform(_p(vg), _p(pg), _p(a))
+        o.or_plain_transform(_p(vg), _p(pg), _p(b))
+        assert np.array_equal(a, b)
+        eye = np.ascontiguousarray(rng.uniform(-500, 500, 3))
+        ce = np.ascontiguousarray(rng.uniform(-50, 50, 3))
+        up = np.array([0.0, 0.0, 1.0])
+        la, lb = np.zeros(16), np.zeros(16)
+        g.glmref_look_at(_p(eye), _p(ce), _p(up), _p(la))
+        o.or_look_at(_p(eye), _p(ce), _p(up), _p(lb))
+        assert np.array_equal(la, lb)
+        assert np.array_equal(synth.look_at(eye, ce, up), la)
+
+
+@pytest.mark.parametrize("n", [1, 10239, 10240, 10241, 33333])
+def test_host_encoder_matches_oracle(n):
+    rec, hdr = synth.las_records_host(synth.synth_params(L.SYNTH_TERRAIN, 300.0, n), n)
+    ours = synth.encode_las(rec, n, hdr, sparse_offset=5, file_index=0)
+    ref = O.encode_las(rec, n, 26, 2, hdr.scale[:], hdr.offset[:], hdr.min[:], sparse_offset=5)
+    for a, b in zip(ours, ref):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    b = ours[0]
+    assert b["num_points"].sum() == n
+    assert (b["first_point"] == 5 + 10240 * np.arange(len(b))).all()
+    # decode at 30 bit stays inside the float AABB's quantisation grid
+    assert (ours[1] >> 30 == 0).all() and (ours[2] >> 30 == 0).all()
+
+
+def test_encoder_zero_extent_axis_and_formats():
+    n = 500
+    rec = np.zeros((n, 34), dtype=np.uint8)
+    xyz = np.stack([np.full(n, 1234), np.arange(n) * 3, np.arange(n) % 7], 1).astype("<i4")
+    rec[:, 0:12] = xyz.view(np.uint8).reshape(n, 12)
+    rgb = np.stack([np.arange(n) * 131 % 65536, np.arange(n) % 256, np.full(n, 300)], 1).astype("<u2")
+    for fmt, off in ((3, 28), (2, 20)):
+        r = rec.copy()
+        r[:, off:off + 6] = rgb.view(np.uint8).reshape(n, 6)
+        r = np.ascontiguousarray(r).reshape(-1)
+        sc, of, bm = [0.01] * 3, [10.0, 20.0, 30.0], [11.0, 19.0, 29.0]
+        lib = L.load()
+        nb = int(lib.cr_num_batches(n))
+        batches = np.zeros(nb, L.BATCH_DTYPE)
+        st = [np.zeros(n, np.uint32) for _ in range(4)]
+        arr = lambda v: np.ascontiguousarray(v, np.float64)
+        sca, ofa, bma = arr(sc), arr(of), arr(bm)
+        assert lib.cr_encode_las(_p(r), n, 34, fmt, _p(sca), _p(ofa), _p(bma), 0, 0, _p(batches),
+                                 *(_p(s) for s in st)) == 0
+        ref = O.encode_las(r, n, 34, fmt, sc, of, bm)
+        assert np.array_equal(batches.view(np.uint8), ref[0].view(np.uint8))
+        for a, b in zip(st, ref[1:]):
+            assert np.array_equal(a, b)
+        assert (st[0] & 1023 == 0).all()  # zero-extent x quantises to 0
+        R = st[3] & 0xFF
+        exp = rgb[:, 0].astype(np.int64)
+        exp = np.where(exp < 256, exp, exp // 256)
+        assert np.array_equal(R, exp)
+
+
+def test_encode_standard_matches_oracle():
+    n = 2000
+    p = synth.synth_params(L.SYNTH_TERRAIN, 100.0, 5)
+    rec, hdr = synth.las_records_host(p, n, morton=False)
+    lib = L.load()
+    v = np.zeros(n, L.VERTEX_DTYPE)
+    sc, of, bm = (np.ascontiguousarray(x[:], np.float64) for x in (hdr.scale, hdr.offset, hdr.min))
+    assert lib.cr_encode_standard(_p(rec), n, 26, 2, _p(sc), _p(of), _p(bm), _p(v)) == 0
+    w = np.zeros(n, L.VERTEX_DTYPE)
+    O.lib().or_encode_standard(_p(rec), n, 26, 2, _p(sc), _p(of), _p(bm), _p(w))
+    assert np.array_equal(v.view(np.uint8), w.view(np.uint8))
+    assert ((v["color"] >> 24) == 255).all()
+
+
+def test_generator_deterministic_and_morton_sorted():
+    p = synth.synth_params(L.SYNTH_TERRAIN_BOXES, 500.0, 11, num_boxes=3, points_per_box=1000)
+    a, ha = synth.las_records_host(p, 20000, morton=False)
+    b, hb = synth.las_records_host(p, 20000, morton=False)
+    assert np.array_equal(a, b)
+    s, hs = synth.las_records_host(p, 20000, morton=True)
+    assert sorted(map(bytes, a.reshape(-1, 26))) == sorted(map(bytes, s.reshape(-1, 26)))
+    xyz = np.frombuffer(s.reshape(-1, 26)[:, :12].tobytes(), "<i4").reshape(-1, 3)
+    pts = xyz * 0.001
+    mn = np.array(hs.min[:])
+    cube = max(hs.max[k] - hs.min[k] for k in range(3))
+    q = np.minimum(((pts - mn) / cube * 2097152.0).astype(np.uint32), 2097151)
+    o = O.lib()
+    codes = [o.or_morton3(int(x), int(y), int(z)) for x, y, z in q]
+    assert all(codes[i] <= codes[i + 1] for i in range(len(codes) - 1))
+    # header bounds are the quantised extremes
+    assert hs.min[0] == xyz[:, 0].min() * 0.001 and hs.max[2] == xyz[:, 2].max() * 0.001
+
+
+def test_quirk_semantics():
+    cl = encoded(n=25000, extent=150.0, seed=3)
+    cam = cameras(cl)["near"]
+    base = oracle_frame(cam, cl["box_min"][None], 0)
+    args = (cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+    fb0 = O.raster_batched(base, *args)
+    fb1 = O.raster_batched(oracle_frame(cam, cl["box_min"][None], O.L0_X12), *args)
+    b = cl["batches"]
+    mins = np.ascontiguousarray(np.stack([b["min_x"], b["min_y"], b["min_z"]], 1), np.float32)
+    maxs = np.ascontiguousarray(np.stack([b["max_x"], b["max_y"], b["max_z"]], 1), np.float32)
+    lv = [O.lib().or_precision_level(C.byref(base), C.byref(base.files[0]), _p(mins[i:i + 1]),
+                                     _p(maxs[i:i + 1])) for i in range(len(b))]
+    assert 0 in lv, "near camera must produce a 30-bit batch"
+    assert not np.array_equal(fb0, fb1), "H1 changes the 30-bit decode"
+    # H2: the inclusive bound also processes local index numPoints; here that is
+    # the zero padding word past N, which decodes to the batch's min corner
+    hm = handmade_cloud([(512, 512, 100), (700, 300, 200), (100, 900, 300)], [1, 2, 3])
+    cam = identity_cam(64, 32)
+    hargs = (hm["batches"], hm["n"], hm["lo"], hm["md"], hm["hi"], hm["rgba"])
+    fa = O.raster_batched(oracle_frame(cam, hm["box_min"][None], 0), *hargs)
+    fb = O.raster_batched(oracle_frame(cam, hm["box_min"][None], O.INCLUSIVE_END), *hargs)
+    diff = np.nonzero(fa != fb)[0]
+    assert len(diff) == 1 and diff[0] == 0 and (int(fb[0]) & 0xFFFFFFFF) == 3
+    assert sum(int(v) != 0xFF800000FF800000 for v in fa) == 3
+    # H3: ceil(numPoints / 10240) records are dispatched, not every record
+    assert O.lib().or_dispatch_batches(12, 10240 * 10 + 5, O.DISPATCH_BY_POINTS) == 11
+    assert O.lib().or_dispatch_batches(12, 10240 * 10 + 5, 0) == 12
+
+
+def test_oracle_threads_equal_scalar():
+    cl = encoded(n=50000, extent=120.0, seed=9)
+    for name, cam in cameras(cl).items():
+        for payload in (O.PAYLOAD_INDEX, O.PAYLOAD_COLOR):
+            fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[L.METHOD_LOOP_LAS], payload)
+            args = (cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+            a = O.raster_batched(fr, *args)
+            b = O.raster_batched(fr, *args, threads=4)
+            assert np.array_equal(a, b), name
+
+
+@pytest.mark.skipif(not GOLDEN.exists(), reason="golden vectors not generated")
+def test_golden_vectors():
+    from golden import make_golden as G
+    g = json.loads(GOLDEN.read_text())
+    for case in g["cases"]:
+        if case.get("cpu_check", True) is False:
+            continue
+        got = G.run_case(case)
+        assert got == case["digests"], case["name"]

@@ -1,0 +1,334 @@
+"""GPU parity: every framebuffer the CUDA path writes is compared bit for bit
+with the oracle's (u64 depth|payload words incl. the guard tail, HQS u32
+depth + u64 accumulators, resolved images), through the C ABI."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from compute_rasterizer_gb300 import _lib as L
+from compute_rasterizer_gb300 import default_params, make_view, synth
+from helpers import (QUIRKS, cameras, encoded, first_diff, gpu_raw, handmade_cloud, identity_cam,
+                     oracle_frame)
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "golden.json"
+
+
+@pytest.fixture(scope="module")
+def small(ctx):
+    cl = encoded(n=62674, extent=200.0, seed=7)
+    cloud = ctx.cloud_from_arrays(cl["batches"], cl["lo"], cl["md"], cl["hi"], cl["rgba"],
+                                  cl["box_min"])
+    return cl, cloud
+
+
+def oracle_fb(cl, cam, method, payload):
+    fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[method], payload)
+    return O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+
+
+@pytest.mark.parametrize("camname", ["far", "near", "mid", "corner"])
+@pytest.mark.parametrize("method,payload", [(L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX),
+                                            (L.METHOD_LOOP_LAS_PREFETCH, L.PAYLOAD_INDEX),
+                                            (L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR),
+                                            (L.METHOD_LOOP_LAS_PREFETCH, L.PAYLOAD_COLOR)])
+def test_batched_fb_and_image(ctx, small, camname, method, payload):
+    cl, cloud = small
+    cam = cameras(cl)[camname]
+    fb, params = gpu_raw(ctx, cloud, cam, method, payload)
+    got = fb.read(L.FB_WORDS)
+    want = oracle_fb(cl, cam, method, payload)
+    assert np.array_equal(got, want), first_diff(got, want)
+    assert (got != L.DEFAULT_CLEAR).sum() > 50
+    ctx.resolve(cloud, params, fb)
+    img = fb.read(L.FB_IMAGE)
+    w, h = cam[2], cam[3]
+    ref = O.resolve_color(w, h, want) if payload else O.resolve_index(w, h, want, cl["rgba"])
+    assert np.array_equal(img, ref), first_diff(img, ref)
+
+
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_block_sizes_agree(ctx, small, block):
+    cl, cloud = small
+    cam = cameras(cl)["near"]
+    fb, _ = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR, block_threads=block,
+                    ctas_per_sm=1)
+    want = oracle_fb(cl, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+    assert np.array_equal(fb.read(L.FB_WORDS), want)
+
+
+@pytest.mark.parametrize("camname", ["far", "near", "mid", "corner"])
+def test_hqs(ctx, small, camname):
+    cl, cloud = small
+    cam = cameras(cl)[camname]
+    fb, params = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS_HQS)
+    fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[L.METHOD_LOOP_LAS_HQS])
+    depth, accum, img = O.hqs(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+    gd = fb.read(L.FB_DEPTH)
+    assert np.array_equal(gd, depth), first_diff(gd, depth)
+    ga = fb.read(L.FB_ACCUM)
+    assert np.array_equal(ga, accum), first_diff(ga, accum)
+    ctx.resolve(cloud, params, fb)
+    gi = fb.read(L.FB_IMAGE)
+    assert np.array_equal(gi, img), first_diff(gi, img)
+
+
+def config1_cam(w, h):
+    view = synth.look_at([150.0, 150.0, 150.0], [50.0, 50.0, 50.0], [0.0, 0.0, 1.0])
+    return view, synth.perspective(60.0, w / h, 0.1, 1000.0), w, h
+
+
+@pytest.mark.parametrize("n,w,h", [(100_000, 320, 180), (4_194_304, 1920, 1080)])
+def test_plain_path(ctx, n, w, h):
+    v = synth.uniform_vertices_host(1, n, 100.0)
+    cloud = ctx.plain_cloud(v)
+    cam = config1_cam(w, h)
+    fb = ctx.framebuffer(w, h)
+    fb.clear(0xFFFFFFFFFFFFFFFF)
+    params = default_params(L.METHOD_EARLYZ, resolve=0, clear_after=0)
+    ctx.render(cloud, make_view(*cam), params, fb)
+    got = fb.read(L.FB_WORDS)
+    want, img, recleared = O.plain(cam[0], cam[1], w, h, v)
+    assert np.array_equal(got, want), first_diff(got, want)
+    params.resolve, params.clear_after = 1, 1
+    ctx.resolve(cloud, params, fb)
+    assert np.array_equal(fb.read(L.FB_IMAGE), img)
+    assert np.array_equal(fb.read(L.FB_WORDS)[:w * h], recleared[:w * h])
+
+
+def test_plain_device_generator_matches_host(ctx):
+    n = 1_000_003
+    cloud = synth.uniform_cloud_device(ctx, 5, n, 100.0)
+    cam = config1_cam(640, 360)
+    fb = ctx.framebuffer(640, 360)
+    fb.clear(0xFFFFFFFFFFFFFFFF)
+    ctx.render(cloud, make_view(*cam), default_params(L.METHOD_EARLYZ, resolve=0, clear_after=0), fb)
+    want, _, _ = O.plain(cam[0], cam[1], 640, 360, synth.uniform_vertices_host(5, n, 100.0))
+    assert np.array_equal(fb.read(L.FB_WORDS), want)
+
+
+@pytest.mark.skipif(not GOLDEN.exists(), reason="no golden vectors")
+def test_golden_digests(ctx):
+    from golden import make_golden as G
+    cases = json.loads(GOLDEN.read_text())["cases"]
+    for case in cases:
+        dg = case["digests"]
+        if case["kind"] == "terrain":
+            hdr, batches, lo, md, hi, rgba = G.terrain_inputs(case)
+            assert G.dg(lo) == dg["low"] and G.dg(rgba) == dg["rgba"]
+            cloud = ctx.cloud_from_arrays(batches, lo, md, hi, rgba, np.array(hdr.min[:]))
+            for cname, c in case["cameras"].items():
+                cam = (G.unhex(c["view"]), G.unhex(c["proj"]), c["width"], c["height"])
+                for m in case["methods"]:
+                    mid = {"loop_las": 0, "loop_las_prefetch": 1, "loop_las_hqs": 2}[m["method"]]
+                    fb, params = gpu_raw(ctx, cloud, cam, mid, m["payload"])
+                    if mid == 2:
+                        assert G.dg(fb.read(L.FB_DEPTH)) == dg[f"{cname}/hqs/depth"]
+                        assert G.dg(fb.read(L.FB_ACCUM)) == dg[f"{cname}/hqs/accum"]
+                        ctx.resolve(cloud, params, fb)
+                        assert G.dg(fb.read(L.FB_IMAGE)) == dg[f"{cname}/hqs/image"]
+                        continue
+                    key = f"{cname}/{m['method']}/{'color' if m['payload'] else 'index'}"
+                    assert G.dg(fb.read(L.FB_WORDS)) == dg[key + "/fb"], key
+                    ctx.resolve(cloud, params, fb)
+                    assert G.dg(fb.read(L.FB_IMAGE)) == dg[key + "/image"], key
+        else:
+            v = synth.uniform_vertices_host(case["seed"], case["n"], case["size"])
+            assert G.dg(v) == dg["vertices"]
+            c = case["camera"]
+            cloud = ctx.plain_cloud(v)
+            fb = ctx.framebuffer(c["width"], c["height"])
+            fb.clear(0xFFFFFFFFFFFFFFFF)
+            p = default_params(L.METHOD_EARLYZ, resolve=0, clear_after=0)
+            ctx.render(cloud, make_view(G.unhex(c["view"]), G.unhex(c["proj"]), c["width"],
+                                        c["height"]), p, fb)
+            assert G.dg(fb.read(L.FB_WORDS)) == dg["fb"], case["name"]
+            p.resolve = 1
+            ctx.resolve(cloud, p, fb)
+            assert G.dg(fb.read(L.FB_IMAGE)) == dg["image"], case["name"]
+
+
+# ---- edge cases -------------------------------------------------------------
+
+def run_handmade(ctx, hm, cam, method, payload=L.PAYLOAD_INDEX, quirks=None):
+    cloud = ctx.cloud_from_arrays(hm["batches"], hm["lo"], hm["md"], hm["hi"], hm["rgba"],
+                                  hm["box_min"])
+    q = QUIRKS.get(method, 0) if quirks is None else quirks
+    fb, _ = gpu_raw(ctx, cloud, cam, method, payload, quirks=q)
+    fr = oracle_frame(cam, hm["box_min"][None], q, payload)
+    want = O.raster_batched(fr, hm["batches"], hm["n"], hm["lo"], hm["md"], hm["hi"], hm["rgba"])
+    return fb.read(L.FB_WORDS), want
+
+
+def test_frustum_edge_writes_guard_row(ctx):
+    s = 1.0 / 1024.0
+    # x == 1 and y == 1 exactly (render.cs:404-409 keeps them): pixel W + H*W
+    hm = handmade_cloud([(1023, 1023, 0), (1023, 500, 0), (0, 1023, 0)], [7, 8, 9],
+                        box_min=(s, s, 0.0), box_max=(1.0 + s, 1.0 + s, 1.0))
+    w, h = 64, 32
+    got, want = run_handmade(ctx, hm, identity_cam(w, h), L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+    assert np.array_equal(got, want), first_diff(got, want)
+    assert (int(got[w * h + w]) & 0xFFFFFFFF) == 7  # last guard entry
+
+
+@pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
+def test_equal_depth_ties_take_min_payload(ctx, payload):
+    pts = [(300, 300, 10)] * 40 + [(301, 300, 10)] * 3
+    colors = list(range(1000, 960, -1)) + [5, 4, 6]
+    hm = handmade_cloud(pts, colors)
+    got, want = run_handmade(ctx, hm, identity_cam(), L.METHOD_LOOP_LAS, payload)
+    assert np.array_equal(got, want)
+
+
+def test_all_culled_frame(ctx, small):
+    cl, cloud = small
+    view = synth.look_at([-5000.0, -5000.0, 100.0], [-10000.0, -10000.0, 100.0], [0, 0, 1.0])
+    cam = (view, synth.perspective(60.0, 4 / 3, 0.1, 200000.0), 320, 240)
+    fb, params = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS)
+    assert (fb.read(L.FB_WORDS) == L.DEFAULT_CLEAR).all()
+    ctx.resolve(cloud, params, fb)
+    assert (fb.read(L.FB_IMAGE) == L.BACKGROUND).all()
+
+
+@pytest.mark.parametrize("pad", [1, 2, 3])
+def test_unaligned_first_point_multi_file(ctx, pad):
+    """Batches of a second file start at a non-multiple of 4 (LasLoaderSparse
+    sparse offsets); the 128-bit loads must mask the neighbours."""
+    a = encoded(n=10240 + pad, extent=60.0, seed=31)
+    b = encoded(n=25000, extent=80.0, seed=32)
+    n = a["n"] + b["n"]
+    bb = b["batches"].copy()
+    bb["first_point"] += a["n"]
+    bb["file_index"] = 1
+    batches = np.concatenate([a["batches"], bb])
+    streams = [np.concatenate([a[k], b[k]]) for k in ("lo", "md", "hi", "rgba")]
+    box = np.stack([a["box_min"], b["box_min"] + np.array([70.0, 0.0, 0.0])])
+    cloud = ctx.cloud_from_arrays(batches, *streams, box)
+    for camname in ("far", "near"):
+        cam = cameras(b)[camname]
+        for method in (L.METHOD_LOOP_LAS, L.METHOD_LOOP_LAS_PREFETCH):
+            fb, _ = gpu_raw(ctx, cloud, cam, method, L.PAYLOAD_INDEX)
+            fr = oracle_frame(cam, box, QUIRKS[method])
+            want = O.raster_batched(fr, batches, n, *streams)
+            got = fb.read(L.FB_WORDS)
+            assert np.array_equal(got, want), (camname, method, first_diff(got, want))
+
+
+def test_hqs_one_pixel_receives_a_million_points(ctx):
+    nb = 98
+    n = nb * 10240
+    lo = np.full(n, 400 | (400 << 10) | (50 << 20), np.uint32)
+    rng = np.random.default_rng(0)
+    rgba = rng.integers(0, 1 << 24, n, dtype=np.uint32)
+    b = np.zeros(nb, L.BATCH_DTYPE)
+    b["min_x"], b["min_y"], b["min_z"] = -1.0, -1.0, 0.0
+    b["max_x"], b["max_y"], b["max_z"] = 1.0, 1.0, 1.0
+    b["num_points"] = 10240
+    b["first_point"] = np.arange(nb) * 10240
+    zeros = np.zeros(n, np.uint32)
+    cloud = ctx.cloud_from_arrays(b, lo, zeros, zeros, rgba, np.zeros(3))
+    cam = identity_cam(64, 32)
+    fb, params = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS_HQS)
+    fr = oracle_frame(cam, np.zeros((1, 3)), QUIRKS[L.METHOD_LOOP_LAS_HQS])
+    depth, accum, img = O.hqs(fr, b, n, lo, zeros, zeros, rgba)
+    ga = fb.read(L.FB_ACCUM)
+    assert np.array_equal(ga, accum)
+    assert (ga[1::2] >> 32).max() == n  # every point counted once (n, not n + 1: full batches)
+    ctx.resolve(cloud, params, fb)
+    assert np.array_equal(fb.read(L.FB_IMAGE), img)
+
+
+def test_resolve_with_clear_restores_every_word(ctx, small):
+    cl, cloud = small
+    cam = cameras(cl)["corner"]
+    fb = ctx.framebuffer(cam[2], cam[3])
+    fb.clear()
+    p = default_params(L.METHOD_LOOP_LAS)
+    ctx.render(cloud, make_view(*cam), p, fb)
+    ctx.sync()
+    assert (fb.read(L.FB_WORDS) == L.DEFAULT_CLEAR).all()
+    # the next frame starts clean: same image twice
+    img1 = fb.read(L.FB_IMAGE)
+    ctx.render(cloud, make_view(*cam), p, fb)
+    assert np.array_equal(fb.read(L.FB_IMAGE), img1)
+
+
+def test_device_flag_on_out_of_range_record(ctx):
+    """A record pointing past the streams is skipped and reported (no fault)."""
+    import torch
+    n = 20480
+    p = synth.synth_params(L.SYNTH_TERRAIN, 100.0, 3)
+    rec = torch.empty(n * 26, dtype=torch.uint8, device="cuda")
+    hdr = L.LasHeader()
+    import ctypes as C
+    lib = L.load()
+    ctx.check(lib.cr_synth_points_device(ctx.handle, C.byref(p), n, rec.data_ptr(), C.byref(hdr),
+                                         None), "gen")
+    cloud = ctx.cloud(n, 2, 1)
+    d = cloud.device_pointers()
+    sc, of, mn = (np.ascontiguousarray(x[:], np.float64) for x in (hdr.scale, hdr.offset, hdr.min))
+    ctx.check(lib.cr_encode_las_device(ctx.handle, rec.data_ptr(), n, 26, 2, sc.ctypes.data,
+                                       of.ctypes.data, mn.ctypes.data, 1_000_000, 0, d["batches"],
+                                       d["low"], d["med"], d["hig"], d["rgba"], None), "encode")
+    cloud.set_files(mn)
+    fb = ctx.framebuffer(64, 64)
+    fb.clear()
+    view = synth.orbit_view(0.5, -0.6, 150.0, mn + 50.0)
+    ctx.render(cloud, make_view(view, synth.perspective(60, 1.0, 0.1, 1e5), 64, 64),
+               default_params(L.METHOD_LOOP_LAS, resolve=0, clear_after=0), fb)
+    with pytest.raises(Exception) as e:
+        ctx.sync()
+    assert getattr(e.value, "status", None) == L.DEVICE_FLAG
+    assert (fb.read(L.FB_WORDS) == L.DEFAULT_CLEAR).all()
+    ctx.sync()  # flag was cleared
+
+
+def test_gpu_generator_sort_encoder_match_host(ctx):
+    import ctypes as C
+
+    import torch
+    lib = L.load()
+    n = 200_001
+    p = synth.synth_params(L.SYNTH_TERRAIN_BOXES, 400.0, 17, num_boxes=4, points_per_box=5000)
+    host, hh = synth.las_records_host(p, n, morton=False)
+    rec = torch.empty(n * 26, dtype=torch.uint8, device="cuda")
+    hd = L.LasHeader()
+    ctx.check(lib.cr_synth_points_device(ctx.handle, C.byref(p), n, rec.data_ptr(), C.byref(hd),
+                                         None), "gen")
+    assert np.array_equal(rec.cpu().numpy(), host)
+    assert list(hd.min) == list(hh.min) and list(hd.max) == list(hh.max)
+    ctx.check(lib.cr_morton_sort_device(ctx.handle, rec.data_ptr(), n, 26, C.byref(hd), None), "sort")
+    sorted_host, _ = synth.las_records_host(p, n, morton=True)
+    assert np.array_equal(rec.cpu().numpy(), sorted_host)
+    ref = synth.encode_las(sorted_host, n, hh)
+    cloud = ctx.cloud(n, len(ref[0]), 1)
+    d = cloud.device_pointers()
+    sc, of, mn = (np.ascontiguousarray(x[:], np.float64) for x in (hd.scale, hd.offset, hd.min))
+    ctx.check(lib.cr_encode_las_device(ctx.handle, rec.data_ptr(), n, 26, 2, sc.ctypes.data,
+                                       of.ctypes.data, mn.ctypes.data, 0, 0, d["batches"], d["low"],
+                                       d["med"], d["hig"], d["rgba"], None), "encode")
+    ctx.sync()
+    assert np.array_equal(cloud.read(0).view(np.uint8), ref[0].view(np.uint8)), "batches"
+    for which, arr in zip((L.STREAM_LOW, L.STREAM_MED, L.STREAM_HIG, L.STREAM_RGBA), ref[1:]):
+        assert np.array_equal(cloud.read(which), arr), which
+
+
+def test_synth_cloud_device_pipeline(ctx):
+    n = 300_000
+    p = synth.synth_params(L.SYNTH_TERRAIN, 500.0, 23)
+    cloud, hdr = synth.build_cloud_device(ctx, p, n)
+    rec, hh = synth.las_records_host(p, n)
+    cl = dict(n=n, batches=None)
+    batches, lo, md, hi, rgba = synth.encode_las(rec, n, hh)
+    assert list(hdr.min) == list(hh.min)
+    cl.update(batches=batches, lo=lo, md=md, hi=hi, rgba=rgba, box_min=np.array(hh.min[:]),
+              box_max=np.array(hh.max[:]))
+    for camname in ("far", "near"):
+        cam = cameras(cl)[camname]
+        fb, _ = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+        want = oracle_fb(cl, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+        assert np.array_equal(fb.read(L.FB_WORDS), want), camname

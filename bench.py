@@ -110,13 +110,14 @@ class Clocks:
 
 
 def cpu_sample(points_full: int, extent_full: float, seed: int, sample: int):
-    """A bounded sample of the workload for the CPU: the corner of the same
-    terrain (same seed, noise wavelength and point density), Morton-sorted and
-    encoded on the host, viewed by the full cloud's camera."""
+    """A bounded sample of the workload for the CPU: the central square of the
+    same terrain (same seed, noise wavelength and point density), Morton-sorted
+    and encoded on the host, viewed by the full cloud's camera."""
     from compute_rasterizer_gb300 import _lib as L
     from compute_rasterizer_gb300 import synth
     ext = extent_full * (sample / points_full) ** 0.5
     p = synth.synth_params(L.SYNTH_TERRAIN, ext, seed, wavelength=extent_full / 4.0)
+    p.origin[0] = p.origin[1] = 0.5 * (extent_full - ext)
     rec, hdr = synth.las_records_host(p, sample)
     enc = encode_parallel(rec, sample, hdr)
     return p, hdr, enc, ext
@@ -181,16 +182,17 @@ def reference_arm(args, world, rank):
     n_full = args.points
     s = min(CPU_SAMPLE_POINTS, n_full)
     p, hdr, enc, ext = cpu_sample(n_full, WORKLOAD["extent"], WORKLOAD["seed"], s)
+    full_min = np.array([0.0, 0.0, hdr.min[2]])
     full_max = np.array([WORKLOAD["extent"], WORKLOAD["extent"], hdr.max[2]])
-    view, proj = camera(np.array(hdr.min[:]), full_max, WORKLOAD["width"], WORKLOAD["height"])
+    view, proj = camera(full_min, full_max, WORKLOAD["width"], WORKLOAD["height"])
     payload = O.PAYLOAD_COLOR if args.payload == "color" else O.PAYLOAD_INDEX
     fr = O.make_frame(view, proj, WORKLOAD["width"], WORKLOAD["height"], np.array(hdr.min[:])[None],
                       1, O.L0_X12, payload)
     cores = os.cpu_count() or 1
     per_frame, frames = time_oracle(fr, enc, s, cores, steps=args.steps, warmup=min(args.warmup, 3))
     v = s / per_frame / 1e9
-    sample = (f"{s:,} points: the {ext:.0f} m corner of the same 10 km terrain at the same density, "
-              f"same camera; oracle {args.steps} frames")
+    sample = (f"{s:,} points: the central {ext:.0f} m square of the same 10 km terrain at the "
+              f"same density, same camera; oracle {args.steps} frames")
     out = {"impl": "reference", "metric": metric_name(), "value": round(v, 4),
            "unit": "Gpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(per_frame * 1e3, 3), "higher_is_better": True, "scaling": "weak",
@@ -398,8 +400,8 @@ def cpu_baseline(args, view, proj):
     per_frame, frames = time_oracle(fr, enc, s, cores, min_seconds=10.0, warmup=1)
     return {"value": round(s / per_frame / 1e9, 4), "unit": "Gpoints/s", "cores": cores,
             "kind": "port",
-            "sample": f"{s:,} points (the {ext:.0f} m corner of the same terrain, same density and "
-                      f"camera), {frames} frames"}
+            "sample": f"{s:,} points (the central {ext:.0f} m square of the same terrain, same "
+                      f"density and camera), {frames} frames"}
 
 
 if __name__ == "__main__":

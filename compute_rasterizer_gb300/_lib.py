@@ -76,7 +76,8 @@ class SynthParams(C.Structure):
                 ("extent", C.c_double), ("height", C.c_double), ("sigma", C.c_double),
                 ("wavelength", C.c_double), ("las_scale", C.c_double),
                 ("num_boxes", C.c_int32), ("points_per_box", C.c_int32),
-                ("box_min_height", C.c_double), ("box_max_height", C.c_double)]
+                ("box_min_height", C.c_double), ("box_max_height", C.c_double),
+                ("origin", C.c_double * 2)]
 
 
 P = C.c_void_p

@@ -178,8 +178,25 @@ struct BatchCtx {
     int32_t W;
 };
 
-// Writes one point's contribution, warp-merged per pixel.  All 32 lanes of
-// the warp call run() together (inactive lanes with ok = false).
+// Early-z reads of the framebuffer go through L1 and may return a stale copy
+// of a word; within a frame every word only decreases, so a stale value is
+// never below the current one: a point it rejects is rejected by the current
+// value too, and a point it passes goes on to the atomic, which decides.
+__device__ __forceinline__ unsigned long long ld_cached_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_cached_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+// Writes one point's contribution.  All 32 lanes of the warp call run()
+// together (inactive lanes with ok = false).  Candidates that pass the early-z
+// read are merged per pixel inside the warp (__match_any_sync, then a min or
+// sum reduction over the peers), and one leader per pixel issues the atomic.
 template <int MODE>
 struct Emit;
 
@@ -187,15 +204,17 @@ template <>
 struct Emit<kModeRaster> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, bool ok, int32_t pix,
                                                uint32_t wbits, uint32_t payload, uint32_t) {
-        uint32_t key_pix = ok ? (uint32_t)pix : kNoPixel;
-        uint32_t peers = __match_any_sync(kFull, key_pix);
-        if (ok) {
-            uint32_t mh = __reduce_min_sync(peers, wbits);
-            uint32_t ml = __reduce_min_sync(peers, wbits == mh ? payload : 0xFFFFFFFFu);
-            if (lane_id() == (uint32_t)(__ffs(peers) - 1)) {
-                unsigned long long key = ((unsigned long long)mh << 32) | ml;
-                unsigned long long* slot = reinterpret_cast<unsigned long long*>(bl.fb) + pix;
-                if (key < *slot) atomicMin(slot, key);
+        unsigned long long* slot = reinterpret_cast<unsigned long long*>(bl.fb) + pix;
+        const unsigned long long key = ((unsigned long long)wbits << 32) | payload;
+        bool cand = false;
+        if (ok) cand = key < ld_cached_u64(slot);  // render.cs:423-424
+        if (__any_sync(kFull, cand)) {
+            const uint32_t peers = __match_any_sync(kFull, cand ? (uint32_t)pix : kNoPixel);
+            if (cand) {
+                const uint32_t mh = __reduce_min_sync(peers, wbits);
+                const uint32_t ml = __reduce_min_sync(peers, wbits == mh ? payload : 0xFFFFFFFFu);
+                if (lane_id() == (uint32_t)(__ffs(peers) - 1))
+                    atomicMin(slot, ((unsigned long long)mh << 32) | ml);
             }
         }
     }
@@ -205,13 +224,14 @@ template <>
 struct Emit<kModeHqsDepth> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, bool ok, int32_t pix,
                                                uint32_t wbits, uint32_t, uint32_t) {
-        uint32_t key_pix = ok ? (uint32_t)pix : kNoPixel;
-        uint32_t peers = __match_any_sync(kFull, key_pix);
-        if (ok) {
-            uint32_t m = __reduce_min_sync(peers, wbits);
-            if (lane_id() == (uint32_t)(__ffs(peers) - 1)) {
-                uint32_t* slot = bl.depth + pix;
-                if (m < *slot) atomicMin(slot, m);
+        uint32_t* slot = bl.depth + pix;
+        bool cand = false;
+        if (ok) cand = wbits < ld_cached_u32(slot);  // hqs/depth.cs:375-379
+        if (__any_sync(kFull, cand)) {
+            const uint32_t peers = __match_any_sync(kFull, cand ? (uint32_t)pix : kNoPixel);
+            if (cand) {
+                const uint32_t m = __reduce_min_sync(peers, wbits);
+                if (lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicMin(slot, m);
             }
         }
     }
@@ -221,23 +241,29 @@ template <>
 struct Emit<kModeHqsColor> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, bool ok, int32_t pix,
                                                uint32_t wbits, uint32_t, uint32_t color) {
-        uint32_t key_pix = ok ? (uint32_t)pix : kNoPixel;
-        uint32_t peers = __match_any_sync(kFull, key_pix);
+        bool vis = false;
         if (ok) {
-            uint32_t leader = __ffs(peers) - 1;
-            uint32_t d = 0;
-            if (lane_id() == leader) d = bl.depth[pix];
-            d = __shfl_sync(peers, d, leader);
+            // the depth buffer is read-only during this pass
+            const uint32_t d = __ldg(bl.depth + pix);
             // color.cs:399-403: depth <= bufferDepth * 1.01
-            bool vis = __uint_as_float(wbits) <= fmul(__uint_as_float(d), 1.01f);
-            uint32_t rg = vis ? ((color & 0xFFu) | (((color >> 8) & 0xFFu) << 16)) : 0u;
-            uint32_t bc = vis ? (((color >> 16) & 0xFFu) | (1u << 16)) : 0u;
-            uint32_t srg = __reduce_add_sync(peers, rg);
-            uint32_t sbc = __reduce_add_sync(peers, bc);
-            if (lane_id() == leader && sbc != 0u) {
-                unsigned long long* a = reinterpret_cast<unsigned long long*>(bl.accum) + 2 * (int64_t)pix;
-                atomicAdd(a, (unsigned long long)(srg & 0xFFFFu) | ((unsigned long long)(srg >> 16) << 32));
-                atomicAdd(a + 1, (unsigned long long)(sbc & 0xFFFFu) | ((unsigned long long)(sbc >> 16) << 32));
+            vis = __uint_as_float(wbits) <= fmul(__uint_as_float(d), 1.01f);
+        }
+        if (__any_sync(kFull, vis)) {
+            // color.cs:408-441: partitioned sums of (R, G, B, 1), leader adds
+            const uint32_t peers = __match_any_sync(kFull, vis ? (uint32_t)pix : kNoPixel);
+            if (vis) {
+                const uint32_t rg = (color & 0xFFu) | (((color >> 8) & 0xFFu) << 16);
+                const uint32_t bc = ((color >> 16) & 0xFFu) | (1u << 16);
+                const uint32_t srg = __reduce_add_sync(peers, rg);
+                const uint32_t sbc = __reduce_add_sync(peers, bc);
+                if (lane_id() == (uint32_t)(__ffs(peers) - 1)) {
+                    unsigned long long* a =
+                        reinterpret_cast<unsigned long long*>(bl.accum) + 2 * (int64_t)pix;
+                    atomicAdd(a, (unsigned long long)(srg & 0xFFFFu) |
+                                     ((unsigned long long)(srg >> 16) << 32));
+                    atomicAdd(a + 1, (unsigned long long)(sbc & 0xFFFFu) |
+                                         ((unsigned long long)(sbc >> 16) << 32));
+                }
             }
         }
     }
@@ -250,7 +276,9 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
     float py = __fmaf_rn(c.T9, z, __fmaf_rn(c.T5, y, __fmaf_rn(c.T1, x, c.T13)));
     float pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
     float qx = __fdiv_rn(px, pw), qy = __fdiv_rn(py, pw);
-    bool in = !(pw <= 0.0f || qx < -1.0f || qx > 1.0f || qy < -1.0f || qy > 1.0f);
+    // render.cs:404 written positively, so a NaN position is outside (the
+    // negated form would keep it and index the framebuffer with garbage)
+    bool in = pw > 0.0f && qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f;
     int32_t ix = small_f2i(fmul(__fmaf_rn(qx, 0.5f, 0.5f), c.Wf));
     int32_t iy = small_f2i(fmul(__fmaf_rn(qy, 0.5f, 0.5f), c.Hf));
     pix = ix + iy * c.W;
@@ -258,32 +286,45 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
     return in;
 }
 
-// LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0)
+// LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0).
+// Points [first, first + count) are read as 128-bit vectors starting at the
+// aligned word below `first`; lanes mask the words outside the range.  The
+// next vector is loaded before the current one is processed.
 template <int MODE, int PAYLOAD, int BLOCK, int LC>
 __device__ __forceinline__ void run_points(const BatchedLaunch& bl, const BatchCtx& c,
-                                           int64_t first, int64_t end, bool l0_x12) {
+                                           int64_t first, int32_t count, bool l0_x12) {
     constexpr bool kNeedColor = (MODE == kModeHqsColor) || (MODE == kModeRaster && PAYLOAD == CR_PAYLOAD_COLOR);
     const int64_t v0 = first >> 2;
-    const int nv = (int)(((end + 3) >> 2) - v0);
+    const int32_t head = (int32_t)(first & 3);
+    const int nv = (head + count + 3) >> 2;
+    const uint32_t index0 = (uint32_t)(first - head);  // global index of word 0 of vector v0
     const uint4* lo4 = reinterpret_cast<const uint4*>(bl.lo) + v0;
     const uint4* md4 = reinterpret_cast<const uint4*>(bl.md) + v0;
     const uint4* hi4 = reinterpret_cast<const uint4*>(bl.hi) + v0;
     const uint4* co4 = reinterpret_cast<const uint4*>(bl.rgba) + v0;
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    uint4 n4 = zero, n8 = zero, n12 = zero, ncol = zero;
+    if ((int)threadIdx.x < nv) {
+        n4 = ld_stream(lo4 + threadIdx.x);
+        if (LC <= 1) n8 = ld_stream(md4 + threadIdx.x);
+        if (LC == 0) n12 = ld_stream(hi4 + threadIdx.x);
+        if (kNeedColor) ncol = ld_stream(co4 + threadIdx.x);
+    }
     for (int base = 0; base < nv; base += BLOCK) {
         const int v = base + (int)threadIdx.x;
-        const bool act = v < nv;
-        uint4 w4 = make_uint4(0, 0, 0, 0), w8 = w4, w12 = w4, col = w4;
-        if (act) {
-            w4 = ld_stream(lo4 + v);
-            if (LC <= 1) w8 = ld_stream(md4 + v);
-            if (LC == 0) w12 = ld_stream(hi4 + v);
-            if (kNeedColor) col = ld_stream(co4 + v);
+        const uint4 w4 = n4, w8 = n8, w12 = n12, col = ncol;
+        const int vn = v + BLOCK;
+        if (vn < nv) {
+            n4 = ld_stream(lo4 + vn);
+            if (LC <= 1) n8 = ld_stream(md4 + vn);
+            if (LC == 0) n12 = ld_stream(hi4 + vn);
+            if (kNeedColor) ncol = ld_stream(co4 + vn);
         }
-        const int64_t idx0 = (v0 + v) * 4;
+        const int32_t rel0 = 4 * v - head;  // batch-local index of word 0
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const int64_t idx = idx0 + j;
-            const bool valid = act && idx >= first && idx < end;
+            const bool valid = (uint32_t)(rel0 + j) < (uint32_t)count;
+            const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
             const uint32_t a = u4get(w4, j);
             float x, y, z;
             if (LC == 2) {
@@ -336,7 +377,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
         const float mnx = __int_as_float(ra.y), mny = __int_as_float(ra.z), mnz = __int_as_float(ra.w);
         const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
         const int64_t first = rd.x;
-        const int64_t end = first + points_in_batch(rc.w, bl.quirks);
+        const int32_t count = (int32_t)points_in_batch(rc.w, bl.quirks);
         const FileRec& f = vp.files[rd.y];
 
         BatchCtx c;
@@ -351,9 +392,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
         c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
         c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
         const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-        if (level >= 2) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, c, first, end, l0_x12);
-        else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, c, first, end, l0_x12);
-        else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, c, first, end, l0_x12);
+        if (level >= 2) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, c, first, count, l0_x12);
+        else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, c, first, count, l0_x12);
+        else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, c, first, count, l0_x12);
         __syncthreads();
         buf ^= 1;
     }

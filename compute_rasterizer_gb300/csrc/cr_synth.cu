@@ -105,8 +105,8 @@ __host__ __device__ inline void gen_point(const cr_synth_params& p, int64_t n, u
     const int64_t nterrain = n - nbox_pts;
     const double inv_wl = 1.0 / p.wavelength;
     if ((int64_t)i < nterrain) {
-        o.x = u53(hash3(p.seed, i, 0)) * p.extent;
-        o.y = u53(hash3(p.seed, i, 1)) * p.extent;
+        o.x = p.origin[0] + u53(hash3(p.seed, i, 0)) * p.extent;
+        o.y = p.origin[1] + u53(hash3(p.seed, i, 1)) * p.extent;
         o.z = p.height * fbm(o.x * inv_wl, o.y * inv_wl, p.seed, p.octaves) + p.sigma * gauss(p.seed, i);
         terrain_color(p, i, o.z, o);
         return;
@@ -114,8 +114,8 @@ __host__ __device__ inline void gen_point(const cr_synth_params& p, int64_t n, u
     // points on the faces of axis-aligned boxes standing on the terrain
     const uint64_t k = i - (uint64_t)nterrain;
     const uint64_t bi = k / (uint64_t)p.points_per_box;
-    const double cx = u53(hash3(p.seed ^ 0xB0C5ull, bi, 0)) * p.extent;
-    const double cy = u53(hash3(p.seed ^ 0xB0C5ull, bi, 1)) * p.extent;
+    const double cx = p.origin[0] + u53(hash3(p.seed ^ 0xB0C5ull, bi, 0)) * p.extent;
+    const double cy = p.origin[1] + u53(hash3(p.seed ^ 0xB0C5ull, bi, 1)) * p.extent;
     const double wx = 10.0 + 30.0 * u53(hash3(p.seed ^ 0xB0C5ull, bi, 2));
     const double wy = 10.0 + 30.0 * u53(hash3(p.seed ^ 0xB0C5ull, bi, 3));
     const double h = p.box_min_height + (p.box_max_height - p.box_min_height) * u53(hash3(p.seed ^ 0xB0C5ull, bi, 4));

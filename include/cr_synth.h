@@ -48,6 +48,7 @@ typedef struct cr_synth_params {
     int32_t points_per_box; /* boxes kind: 20000 */
     double box_min_height;  /* 10 */
     double box_max_height;  /* 60 */
+    double origin[2];       /* x, y of the square's corner (0, 0); the height field is absolute */
 } cr_synth_params;
 
 void cr_synth_params_default(int32_t kind, double extent, uint64_t seed, cr_synth_params* out);

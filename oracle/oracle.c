@@ -303,9 +303,11 @@ static int project(const float T[16], int32_t W, int32_t H, const float p[3], in
     float x = fmaf(T[8], p[2], fmaf(T[4], p[1], fmaf(T[0], p[0], T[12])));
     float y = fmaf(T[9], p[2], fmaf(T[5], p[1], fmaf(T[1], p[0], T[13])));
     float w = fmaf(T[11], p[2], fmaf(T[7], p[1], fmaf(T[3], p[0], T[15])));
-    if (w <= 0.0f) return 0;
+    /* render.cs:404 `!(w <= 0 || x < -1 || ...)`, written positively so that
+     * a NaN position counts as outside */
+    if (!(w > 0.0f)) return 0;
     float qx = x / w, qy = y / w;
-    if (qx < -1.0f || qx > 1.0f || qy < -1.0f || qy > 1.0f) return 0;
+    if (!(qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f)) return 0;
     float fx = fmaf(qx, 0.5f, 0.5f) * (float)W;
     float fy = fmaf(qy, 0.5f, 0.5f) * (float)H;
     int32_t px = (int32_t)fx, py = (int32_t)fy;

@@ -26,7 +26,7 @@
  *       x  = fma(float(X), boxSize.x / STEPS, min.x)      (STEPS = 2^10 or 2^30)
  *       p.c = fma(T[2][c], z, fma(T[1][c], y, fma(T[0][c], x, T[3][c])))  c = x, y, w
  *       q  = p.x / p.w, p.y / p.w                          (correctly rounded)
- *       inside = !(w <= 0 || qx < -1 || qx > 1 || qy < -1 || qy > 1)
+ *       inside = w > 0 && -1 <= qx <= 1 && -1 <= qy <= 1   (NaN is outside)
  *       px = int(fma(qx, 0.5, 0.5) * float(W))  (truncation; same for y/H)
  *       pixel = px + py * W
  *     p.z is never used by the reference (only its division), so it is not formed.

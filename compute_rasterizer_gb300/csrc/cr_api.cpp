@@ -694,7 +694,8 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     bl.scratch = ctx->scratch;
     bl.quirks = quirks;
     bl.payload = hqs ? CR_PAYLOAD_INDEX : p->payload;
-    const int block = (p->block_threads == 128 || p->block_threads == 512) ? p->block_threads : 256;
+    // 128 threads per CTA measured fastest for every payload at 1B points
+    const int block = (p->block_threads == 256 || p->block_threads == 512) ? p->block_threads : 128;
     const int modes[2] = {hqs ? kModeHqsDepth : kModeRaster, kModeHqsColor};
     for (int pass = 0; pass < 2; pass++) {
         if (pass == 1 && !hqs) {

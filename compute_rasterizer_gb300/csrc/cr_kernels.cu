@@ -193,54 +193,114 @@ __device__ __forceinline__ uint32_t ld_cached_u32(const uint32_t* p) {
     return v;
 }
 
+// Per-CTA early-z cache in shared memory: a direct-mapped table (Fibonacci
+// hash of the pixel id) of words `depth << 32 | pixel`.  Every depth stored is
+// one this CTA submitted to, or read from, the framebuffer during the frame, so
+// it is never below the pixel's final minimum depth: a point deeper than the
+// cached depth of its pixel cannot win and is dropped without touching global
+// memory.  Entries are single 64-bit words, so a racing writer replaces an
+// entry but never tears one; the table starts empty (pixel 0xFFFFFFFF).
+constexpr int kZCacheBits = 11;
+constexpr int kZCacheSlots = 1 << kZCacheBits;
+
+__device__ __forceinline__ uint32_t zslot(int32_t pix) {
+    return ((uint32_t)pix * 2654435761u) >> (32 - kZCacheBits);
+}
+
 // Writes one point's contribution.  All 32 lanes of the warp call run()
-// together (inactive lanes with ok = false).  Candidates that pass the early-z
-// read are merged per pixel inside the warp (__match_any_sync, then a min or
+// together (inactive lanes with ok = false).  Points that survive the early-z
+// test are merged per pixel inside the warp (__match_any_sync, then a min or
 // sum reduction over the peers), and one leader per pixel issues the atomic.
 template <int MODE>
 struct Emit;
 
+// Leader side of the raster / depth passes: submit `key` for `pix` and record
+// the pixel's new upper bound in the cache.  On a cache miss the framebuffer
+// word is read first (a possibly stale L1 copy, which is still an upper bound)
+// so that a point behind the stored minimum issues no atomic.
+template <typename T>
+__device__ __forceinline__ void submit_min(T* gslot, unsigned long long* zc, uint32_t slot,
+                                           int32_t pix, T key, uint32_t depth_of_key);
+
+template <>
+__device__ __forceinline__ void submit_min<unsigned long long>(unsigned long long* g,
+                                                               unsigned long long* zc,
+                                                               uint32_t slot, int32_t pix,
+                                                               unsigned long long key,
+                                                               uint32_t kd) {
+    const unsigned long long e = zc[slot];
+    uint32_t bound = kd;
+    if ((uint32_t)e == (uint32_t)pix) {
+        atomicMin(g, key);
+    } else {
+        const unsigned long long cur = ld_cached_u64(g);
+        if (key < cur) atomicMin(g, key);
+        else bound = (uint32_t)(cur >> 32);
+    }
+    zc[slot] = ((unsigned long long)bound << 32) | (uint32_t)pix;
+}
+
+template <>
+__device__ __forceinline__ void submit_min<uint32_t>(uint32_t* g, unsigned long long* zc,
+                                                     uint32_t slot, int32_t pix, uint32_t key,
+                                                     uint32_t kd) {
+    const unsigned long long e = zc[slot];
+    uint32_t bound = kd;
+    if ((uint32_t)e == (uint32_t)pix) {
+        atomicMin(g, key);
+    } else {
+        const uint32_t cur = ld_cached_u32(g);
+        if (key < cur) atomicMin(g, key);
+        else bound = cur;
+    }
+    zc[slot] = ((unsigned long long)bound << 32) | (uint32_t)pix;
+}
+
+__device__ __forceinline__ bool zcache_rejects(const unsigned long long* zc, uint32_t slot,
+                                               int32_t pix, uint32_t wbits) {
+    const unsigned long long e = zc[slot];
+    return (uint32_t)e == (uint32_t)pix && wbits > (uint32_t)(e >> 32);
+}
+
+// The raster and depth passes merge same-pixel candidates through the CTA's
+// z-cache rather than with __match_any_sync: a warp vote skips the atomic path
+// when no lane survives the cache test, and each surviving lane submits its
+// own 64-bit (or 32-bit) atomic min.  Measured on 1B points, a match-and-reduce
+// merge in front of the atomics made the frame 6-11% slower at every
+// threshold tried.
 template <>
 struct Emit<kModeRaster> {
-    static __device__ __forceinline__ void run(const BatchedLaunch& bl, bool ok, int32_t pix,
-                                               uint32_t wbits, uint32_t payload, uint32_t) {
-        unsigned long long* slot = reinterpret_cast<unsigned long long*>(bl.fb) + pix;
-        const unsigned long long key = ((unsigned long long)wbits << 32) | payload;
-        bool cand = false;
-        if (ok) cand = key < ld_cached_u64(slot);  // render.cs:423-424
-        if (__any_sync(kFull, cand)) {
-            const uint32_t peers = __match_any_sync(kFull, cand ? (uint32_t)pix : kNoPixel);
-            if (cand) {
-                const uint32_t mh = __reduce_min_sync(peers, wbits);
-                const uint32_t ml = __reduce_min_sync(peers, wbits == mh ? payload : 0xFFFFFFFFu);
-                if (lane_id() == (uint32_t)(__ffs(peers) - 1))
-                    atomicMin(slot, ((unsigned long long)mh << 32) | ml);
-            }
-        }
+    static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long* zc,
+                                               bool ok, int32_t pix, uint32_t wbits,
+                                               uint32_t payload, uint32_t) {
+        const uint32_t slot = zslot(pix);
+        // render.cs:423-424 early depth test, against the CTA's cache
+        const bool cand = ok && !zcache_rejects(zc, slot, pix, wbits);
+        if (__any_sync(kFull, cand) && cand)
+            submit_min<unsigned long long>(reinterpret_cast<unsigned long long*>(bl.fb) + pix, zc,
+                                           slot, pix, ((unsigned long long)wbits << 32) | payload,
+                                           wbits);
     }
 };
 
 template <>
 struct Emit<kModeHqsDepth> {
-    static __device__ __forceinline__ void run(const BatchedLaunch& bl, bool ok, int32_t pix,
-                                               uint32_t wbits, uint32_t, uint32_t) {
-        uint32_t* slot = bl.depth + pix;
-        bool cand = false;
-        if (ok) cand = wbits < ld_cached_u32(slot);  // hqs/depth.cs:375-379
-        if (__any_sync(kFull, cand)) {
-            const uint32_t peers = __match_any_sync(kFull, cand ? (uint32_t)pix : kNoPixel);
-            if (cand) {
-                const uint32_t m = __reduce_min_sync(peers, wbits);
-                if (lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicMin(slot, m);
-            }
-        }
+    static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long* zc,
+                                               bool ok, int32_t pix, uint32_t wbits, uint32_t,
+                                               uint32_t) {
+        const uint32_t slot = zslot(pix);
+        // hqs/depth.cs:375-379
+        const bool cand = ok && !zcache_rejects(zc, slot, pix, wbits);
+        if (__any_sync(kFull, cand) && cand)
+            submit_min<uint32_t>(bl.depth + pix, zc, slot, pix, wbits, wbits);
     }
 };
 
 template <>
 struct Emit<kModeHqsColor> {
-    static __device__ __forceinline__ void run(const BatchedLaunch& bl, bool ok, int32_t pix,
-                                               uint32_t wbits, uint32_t, uint32_t color) {
+    static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long*,
+                                               bool ok, int32_t pix, uint32_t wbits, uint32_t,
+                                               uint32_t color) {
         bool vis = false;
         if (ok) {
             // the depth buffer is read-only during this pass
@@ -291,8 +351,9 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
 // aligned word below `first`; lanes mask the words outside the range.  The
 // next vector is loaded before the current one is processed.
 template <int MODE, int PAYLOAD, int BLOCK, int LC>
-__device__ __forceinline__ void run_points(const BatchedLaunch& bl, const BatchCtx& c,
-                                           int64_t first, int32_t count, bool l0_x12) {
+__device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned long long* zc,
+                                           const BatchCtx& c, int64_t first, int32_t count,
+                                           bool l0_x12) {
     constexpr bool kNeedColor = (MODE == kModeHqsColor) || (MODE == kModeRaster && PAYLOAD == CR_PAYLOAD_COLOR);
     const int64_t v0 = first >> 2;
     const int32_t head = (int32_t)(first & 3);
@@ -351,7 +412,7 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, const BatchC
             const bool ok = project(c, x, y, z, pix, wbits) && valid;
             const uint32_t color = kNeedColor ? u4get(col, j) : 0u;
             const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? color : (uint32_t)idx;
-            Emit<MODE>::run(bl, ok, pix, wbits, payload, color);
+            Emit<MODE>::run(bl, zc, ok, pix, wbits, payload, color);
         }
     }
 }
@@ -359,8 +420,11 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, const BatchC
 template <int MODE, int PAYLOAD, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch bl) {
     __shared__ uint32_t s_item[2];
+    __shared__ unsigned long long s_zc[MODE == kModeHqsColor ? 1 : kZCacheSlots];
     uint32_t* cursor = bl.scratch + (MODE == kModeHqsColor ? kCursor1 : kCursor0);
     const uint32_t nitems = *reinterpret_cast<volatile uint32_t*>(bl.scratch + kItemCount);
+    if (MODE != kModeHqsColor)
+        for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
     if (threadIdx.x == 0) s_item[0] = atomicAdd(cursor, 1u);
     __syncthreads();
     int buf = 0;
@@ -392,9 +456,9 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
         c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
         c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
         const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-        if (level >= 2) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, c, first, count, l0_x12);
-        else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, c, first, count, l0_x12);
-        else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, c, first, count, l0_x12);
+        if (level >= 2) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
+        else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, first, count, l0_x12);
+        else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, first, count, l0_x12);
         __syncthreads();
         buf ^= 1;
     }
@@ -418,6 +482,9 @@ __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __
     c.Wf = (float)pp.W; c.Hf = (float)pp.H; c.W = pp.W;
     BatchedLaunch bl{};
     bl.fb = fb;
+    __shared__ unsigned long long s_zc[kZCacheSlots];
+    for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
+    __syncthreads();
     const int64_t stride = (int64_t)gridDim.x * BLOCK;
     for (int64_t base = (int64_t)blockIdx.x * BLOCK; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
@@ -428,7 +495,7 @@ __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __
         uint32_t wbits;
         const bool ok = project(c, __uint_as_float(p.x), __uint_as_float(p.y), __uint_as_float(p.z),
                                 pix, wbits) && act;
-        Emit<kModeRaster>::run(bl, ok, pix, wbits, p.w, 0u);
+        Emit<kModeRaster>::run(bl, s_zc, ok, pix, wbits, p.w, 0u);
     }
 }
 

@@ -117,6 +117,8 @@ _SIGS = {
     "cr_fb_device": (I32, [P, I32, PP]),
     "cr_render": (I32, [P, P, C.POINTER(View), C.POINTER(RenderParams), P, P]),
     "cr_resolve": (I32, [P, P, C.POINTER(RenderParams), P, P]),
+    "cr_render_batched_noalloc": (I32, [P, I64, I64, P, P, P, P, I64, P, I32, C.POINTER(View),
+                                        C.POINTER(RenderParams), P, P]),
     "cr_timing_enable": (I32, [P, I32]),
     "cr_timing_read": (I32, [P, I32, C.POINTER(C.c_float), I32]),
     "cr_last_frame_stats": (I32, [P, P, C.POINTER(RenderParams), C.POINTER(FrameStats)]),

@@ -215,6 +215,23 @@ int read_u16(const uint8_t* p) { uint16_t v; std::memcpy(&v, p, 2); return v; }
 
 }  // namespace
 
+cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
+                              int32_t culling, ViewParams* vp) {
+    if (!view || !box_min || !vp || num_files < 1 || num_files > kInlineFiles)
+        return CR_ERR_INVALID_ARG;
+    if (!finite_all(view->view, 16) || !finite_all(view->proj, 16) ||
+        !finite_all(box_min, 3 * num_files))
+        return CR_ERR_INVALID_ARG;
+    std::memset(vp, 0, sizeof(*vp));
+    for (int i = 0; i < 16; i++) vp->P[i] = (float)view->proj[i];
+    vp->W = view->width;
+    vp->H = view->height;
+    vp->nfiles = num_files;
+    vp->culling = culling ? 1 : 0;
+    for (int f = 0; f < num_files; f++) file_record(view->view, view->proj, &box_min[3 * f], &vp->files[f]);
+    return CR_OK;
+}
+
 // ============================================================================
 extern "C" {
 

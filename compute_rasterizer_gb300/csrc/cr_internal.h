@@ -86,5 +86,10 @@ int launch_resolve_hqs(int32_t W, int32_t H, uint32_t* depth, uint64_t* accum, u
                        int clear_after, void* stream);
 int launch_fill_u64(uint64_t* p, int64_t n, uint64_t v, void* stream);
 int launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, void* stream);
+int batched_blocks_per_sm(int mode, int payload, int block);
+
+// Per-view uniforms from double matrices and per-file boxMin (cr_api.cpp).
+cr_status view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
+                          int32_t culling, ViewParams* out);
 
 }  // namespace cr

@@ -193,6 +193,36 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
 cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params* params,
                      cr_fb* fb, void* stream);
 
+/* ---- rasterizing without allocating ------------------------------------------
+ * No counterpart in the reference (its Methods own GL buffers created at
+ * start-up).  For callers that must not allocate device memory while they
+ * render: a host engine that owns the GPU memory budget, a plugin running
+ * inside someone else's frame loop, or code that records work into a CUDA
+ * graph, where cudaMalloc/cudaFree synchronise the device or are not allowed.
+ * Same cull + raster as cr_render for the batched methods (loop_las,
+ * loop_las_prefetch; no resolve, no HQS) on caller-owned device buffers; its
+ * work list lives in a fixed device array inside the library, sized for at
+ * most CR_NOALLOC_MAX_BATCHES batch records (512 KB, held on every GPU that
+ * loads the library until the process exits).  It allocates nothing: no
+ * cudaMalloc, cudaFree or allocating library call.
+ *   - `fb` holds width*height + width + 1 words, already cleared by the caller.
+ *   - streams hold `stream_words` words each, with at least 64 zeroed words
+ *     past the last point (the padding cr_cloud_create adds).
+ *   - The first call on a device looks up the array's device address (once per
+ *     device, with that device current); make that first call before any
+ *     stream capture.
+ *   - Every call shares the one array, so calls whose work overlaps on the GPU
+ *     (other streams, other threads) race; serialise them on one stream.
+ * Returns CR_ERR_INVALID_ARG past the size limit or for bad arguments. */
+#define CR_NOALLOC_MAX_BATCHES 131064
+cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_t num_batches,
+                                    int64_t num_points, const uint32_t* d_xyz_low,
+                                    const uint32_t* d_xyz_med, const uint32_t* d_xyz_hig,
+                                    const uint32_t* d_rgba, int64_t stream_words,
+                                    const double* file_box_min, int32_t num_files,
+                                    const cr_view* view, const cr_render_params* params,
+                                    uint64_t* d_fb, void* stream);
+
 /* ---- timer queries and frame counters --------------------------------------
  * GLTimerQueries::timestamp pairs (src/GLTimerQueries.cpp:6-22) around the
  * dispatches become CUDA events: while timing is on, every cr_render records

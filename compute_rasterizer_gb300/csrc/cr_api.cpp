@@ -117,9 +117,11 @@ void frustum_planes(const float* m, float* planes) {
     for (int i = 0; i < 6; i++) {
         const float* p = comb[i];
         float len = std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
-        planes[4 * i + 0] = p[0] / len;
-        planes[4 * i + 1] = p[1] / len;
-        planes[4 * i + 2] = p[2] / len;
+        // render.cs:139-140: vec3 / length is one reciprocal, w / length a division
+        const float inv = 1.0f / len;
+        planes[4 * i + 0] = p[0] * inv;
+        planes[4 * i + 1] = p[1] * inv;
+        planes[4 * i + 2] = p[2] * inv;
         planes[4 * i + 3] = p[3] / len;
     }
 }

@@ -1,9 +1,12 @@
 // cr_kernels.cu -- sm_103a kernels of the point-rasterizer hot path.
 //
 // Compiled with -fmad=false: every fused multiply-add below is an explicit
-// __fmaf_rn, every other float operation rounds on its own, and / and sqrt are
-// IEEE (__fdiv_rn, __fsqrt_rn).  The operation order follows the arithmetic
-// contract the oracle states, which is what makes the framebuffers bit-exact.
+// __fmaf_rn, every other float operation rounds on its own, scalar / and sqrt
+// are IEEE (__fdiv_rn, __fsqrt_rn), and a vector divided by a scalar is a
+// multiplication by the scalar's correctly rounded reciprocal (__frcp_rn), the
+// one reciprocal a shader compiler emits for it.  The operation order follows
+// the arithmetic contract the oracle states, which is what makes the
+// framebuffers bit-exact.
 //
 // Kernels
 //   k_cull      one thread per batch record: validation, frustum cull
@@ -12,12 +15,11 @@
 //   k_batched   persistent CTAs pull work items; per batch the points are read
 //               with 128-bit streaming loads (4 consecutive points per lane,
 //               the loop_las2 `uvec4` scheme), decoded at 10/20/30 bit,
-//               projected, and merged per pixel inside the warp with
-//               __match_any_sync + __reduce_min_sync before one 64-bit
-//               atomicMin per distinct pixel (render.cs:399-432).  The same
-//               body runs the HQS depth pass (u32 atomicMin, hqs/depth.cs)
-//               and color pass (partitioned sums + two 64-bit atomicAdd,
-//               hqs/color.cs:388-444).
+//               projected, tested against a per-CTA shared-memory z-cache,
+//               and the survivors issue 64-bit atomicMin (render.cs:399-432).
+//               The same body runs the HQS depth pass (u32 atomicMin,
+//               hqs/depth.cs) and color pass (__match_any_sync partitioned
+//               sums + two 64-bit atomicAdd per pixel, hqs/color.cs:388-444).
 //   k_plain     16 B/point path (compute_2021_earlyz/render.cs:35-74).
 //   k_resolve_* per-pixel resolves (resolve.cs files), optionally re-clearing.
 #include <cuda_runtime.h>
@@ -105,8 +107,10 @@ __device__ int precision_level(const float* P, const float* VW, int32_t W, int32
     ve[3] = fadd(vc[3], 0.0f);
     mat4_vec4(P, vc, pc);
     mat4_vec4(P, ve, pe);
-    float pcx = __fdiv_rn(pc[0], pc[3]), pcy = __fdiv_rn(pc[1], pc[3]);
-    float pex = __fdiv_rn(pe[0], pe[3]), pey = __fdiv_rn(pe[1], pe[3]);
+    // render.cs:210-211 `xy / w`: one correctly rounded reciprocal per vector
+    const float rc = __frcp_rn(pc[3]), re = __frcp_rn(pe[3]);
+    float pcx = fmul(pc[0], rc), pcy = fmul(pc[1], rc);
+    float pex = fmul(pe[0], re), pey = fmul(pe[1], re);
     float Wf = (float)W, Hf = (float)H;
     float scx = __fdiv_rn(fmul(Wf, fadd(pcx, 1.0f)), 2.0f);
     float scy = __fdiv_rn(fmul(Hf, fadd(pcy, 1.0f)), 2.0f);
@@ -335,7 +339,9 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
     float px = __fmaf_rn(c.T8, z, __fmaf_rn(c.T4, y, __fmaf_rn(c.T0, x, c.T12)));
     float py = __fmaf_rn(c.T9, z, __fmaf_rn(c.T5, y, __fmaf_rn(c.T1, x, c.T13)));
     float pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
-    float qx = __fdiv_rn(px, pw), qy = __fdiv_rn(py, pw);
+    // render.cs:402 `pos.xyz / pos.w`: one correctly rounded reciprocal of w
+    const float rw = __frcp_rn(pw);
+    float qx = fmul(px, rw), qy = fmul(py, rw);
     // render.cs:404 written positively, so a NaN position is outside (the
     // negated form would keep it and index the framebuffer with garbage)
     bool in = pw > 0.0f && qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f;

@@ -162,9 +162,10 @@ void or_orbit_world(double yaw, double pitch, double radius, const double target
 /* render.cs:134-143 createPlane + :145-174 frustumPlanes. */
 static void create_plane(float x, float y, float z, float w, float out[4]) {
     float len = sqrtf((x * x + y * y) + z * z);
-    out[0] = x / len;
-    out[1] = y / len;
-    out[2] = z / len;
+    float inv = 1.0f / len; /* vec3(x, y, z) / nLength: one reciprocal */
+    out[0] = x * inv;
+    out[1] = y * inv;
+    out[2] = z * inv;
     out[3] = w / len;
 }
 
@@ -239,8 +240,9 @@ int or_precision_level(const or_frame* fr, const or_file_frame* file, const floa
     ve[0] = vc[0] + radius; ve[1] = vc[1] + 0.0f; ve[2] = vc[2] + 0.0f; ve[3] = vc[3] + 0.0f;
     mat4_vec4(fr->proj, vc, pc);
     mat4_vec4(fr->proj, ve, pe);
-    float pcx = pc[0] / pc[3], pcy = pc[1] / pc[3];
-    float pex = pe[0] / pe[3], pey = pe[1] / pe[3];
+    float rc = 1.0f / pc[3], re = 1.0f / pe[3]; /* xy / w: one reciprocal each */
+    float pcx = pc[0] * rc, pcy = pc[1] * rc;
+    float pex = pe[0] * re, pey = pe[1] * re;
     float W = (float)fr->width, H = (float)fr->height;
     float scx = (W * (pcx + 1.0f)) / 2.0f, scy = (H * (pcy + 1.0f)) / 2.0f;
     float sex = (W * (pex + 1.0f)) / 2.0f, sey = (H * (pey + 1.0f)) / 2.0f;
@@ -306,7 +308,8 @@ static int project(const float T[16], int32_t W, int32_t H, const float p[3], in
     /* render.cs:404 `!(w <= 0 || x < -1 || ...)`, written positively so that
      * a NaN position counts as outside */
     if (!(w > 0.0f)) return 0;
-    float qx = x / w, qy = y / w;
+    float rw = 1.0f / w; /* pos.xyz / pos.w: one reciprocal of w */
+    float qx = x * rw, qy = y * rw;
     if (!(qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f)) return 0;
     float fx = fmaf(qx, 0.5f, 0.5f) * (float)W;
     float fy = fmaf(qy, 0.5f, 0.5f) * (float)H;

@@ -15,7 +15,9 @@
  * driver; this contract fixes them, and the CUDA kernels follow it bit for bit):
  *   - IEEE binary32/binary64, round-to-nearest-even, no implicit contraction
  *     (compiled with -ffp-contract=off); every FMA below is written explicitly.
- *   - x / y, sqrt: correctly rounded.
+ *   - scalar x / y and sqrt: correctly rounded.  A vector divided by a scalar
+ *     (v / s in GLSL) is v * RN(1/s): one correctly rounded reciprocal,
+ *     multiplied into each component, which is how shader compilers emit it.
  *   - matrix * matrix (glm order): R[c][r] = ((A[0][r]*B[c][0] + A[1][r]*B[c][1])
  *     + A[2][r]*B[c][2]) + A[3][r]*B[c][3]; no FMA.  Matrices are column-major,
  *     element (c, r) stored at [c*4 + r].
@@ -25,7 +27,7 @@
  *   - per-point math (decode + project), explicit FMA:
  *       x  = fma(float(X), boxSize.x / STEPS, min.x)      (STEPS = 2^10 or 2^30)
  *       p.c = fma(T[2][c], z, fma(T[1][c], y, fma(T[0][c], x, T[3][c])))  c = x, y, w
- *       q  = p.x / p.w, p.y / p.w                          (correctly rounded)
+ *       r  = 1 / p.w (correctly rounded);  q = p.x * r, p.y * r
  *       inside = w > 0 && -1 <= qx <= 1 && -1 <= qy <= 1   (NaN is outside)
  *       px = int(fma(qx, 0.5, 0.5) * float(W))  (truncation; same for y/H)
  *       pixel = px + py * W

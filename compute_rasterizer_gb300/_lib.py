@@ -119,6 +119,16 @@ _SIGS = {
     "cr_resolve": (I32, [P, P, C.POINTER(RenderParams), P, P]),
     "cr_render_batched_noalloc": (I32, [P, I64, I64, P, P, P, P, I64, P, I32, C.POINTER(View),
                                         C.POINTER(RenderParams), P, P]),
+    "cr_mv_create": (I32, [P, P, I32, P, P, C.POINTER(RenderParams), PP]),
+    "cr_mv_destroy": (I32, [P]),
+    "cr_mv_last_error": (C.c_char_p, [P]),
+    "cr_mv_set_params": (I32, [P, C.POINTER(RenderParams)]),
+    "cr_mv_get_params": (I32, [P, C.POINTER(RenderParams)]),
+    "cr_mv_set_views": (I32, [P, C.POINTER(View)]),
+    "cr_mv_render": (I32, [P, I32, P]),
+    "cr_mv_clear": (I32, [P, U64, P]),
+    "cr_mv_read": (I32, [P, I32, I32, P, I64, P]),
+    "cr_mv_autotune": (I32, [P, I32, P, C.POINTER(RenderParams), C.c_char_p, I32]),
     "cr_timing_enable": (I32, [P, I32]),
     "cr_timing_read": (I32, [P, I32, C.POINTER(C.c_float), I32]),
     "cr_last_frame_stats": (I32, [P, P, C.POINTER(RenderParams), C.POINTER(FrameStats)]),

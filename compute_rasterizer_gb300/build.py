@@ -17,7 +17,7 @@ OUT = PKG / "_build"
 LIB = OUT / "libcr_raster.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-SOURCES = ["cr_api.cpp", "cr_kernels.cu", "cr_synth.cu", "cr_noalloc.cu"]
+SOURCES = ["cr_api.cpp", "cr_kernels.cu", "cr_synth.cu", "cr_noalloc.cu", "cr_multiview.cu"]
 
 # -fmad=false: no implicit contraction; explicit __fmaf_rn only.
 NVCC_FLAGS = [
@@ -47,7 +47,7 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
     """Compile and link libcr_raster.so; returns its path."""
     OUT.mkdir(parents=True, exist_ok=True)
     srcs = [CSRC / s for s in SOURCES]
-    deps = srcs + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "cr_raster.h",
+    deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "cr_raster.h",
                                             PKG.parent / "include" / "cr_synth.h"]
     if LIB.exists() and not force and not verbose_ptxas:
         newest = max(p.stat().st_mtime for p in deps if p.exists())

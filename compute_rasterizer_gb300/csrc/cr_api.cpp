@@ -217,6 +217,23 @@ int read_u16(const uint8_t* p) { uint16_t v; std::memcpy(&v, p, 2); return v; }
 
 }  // namespace
 
+bool cr::cloud_info(const cr_cloud* c, CloudInfo* out) {
+    if (!c || !out || c->plain) return false;
+    out->batches = c->batches;
+    out->lo = c->lo;
+    out->md = c->md;
+    out->hi = c->hi;
+    out->rgba = c->rgba;
+    out->n = c->n;
+    out->nb = c->nb;
+    out->capacity = c->capacity;
+    out->nfiles = c->nfiles;
+    out->box_min = c->box_min.data();
+    return true;
+}
+
+int cr::default_quirks_for(int32_t method) { return default_quirks(method); }
+
 cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
                               int32_t culling, ViewParams* vp) {
     if (!view || !box_min || !vp || num_files < 1 || num_files > kInlineFiles)
@@ -711,6 +728,7 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     bl.depth = fb->depth;
     bl.accum = fb->accum;
     bl.scratch = ctx->scratch;
+    bl.list_cap = nb;
     bl.quirks = quirks;
     bl.payload = hqs ? CR_PAYLOAD_INDEX : p->payload;
     // 128 threads per CTA measured fastest for every payload at 1B points
@@ -742,12 +760,18 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
     if (!ctx || !cloud || !p || !out || cloud->plain) return CR_ERR_INVALID_ARG;
     std::memset(out, 0, sizeof(*out));
     CR_CUDA(ctx, cudaDeviceSynchronize(), "synchronize");
-    uint32_t count = 0;
-    CR_CUDA(ctx, cudaMemcpy(&count, ctx->scratch + kItemCount, 4, cudaMemcpyDeviceToHost), "count read");
+    uint32_t counts[kCounterWords] = {};
+    CR_CUDA(ctx, cudaMemcpy(counts, ctx->scratch, sizeof(counts), cudaMemcpyDeviceToHost), "count read");
+    const uint32_t n_front = counts[kItemCount], n_back = counts[kItemCount2];
+    const uint32_t count = n_front + n_back;
     std::vector<uint32_t> items(count);
-    if (count)
-        CR_CUDA(ctx, cudaMemcpy(items.data(), ctx->scratch + kScratchHead, (size_t)count * 4,
+    if (n_front)
+        CR_CUDA(ctx, cudaMemcpy(items.data(), ctx->scratch + kScratchHead, (size_t)n_front * 4,
                                 cudaMemcpyDeviceToHost), "item read");
+    if (n_back)  // the 20/30-bit list fills the region from its end
+        CR_CUDA(ctx, cudaMemcpy(items.data() + n_front,
+                                ctx->scratch + kScratchHead + ctx->last_dispatched - n_back,
+                                (size_t)n_back * 4, cudaMemcpyDeviceToHost), "item read");
     std::vector<cr_batch> recs((size_t)cloud->nb);
     if (cloud->nb)
         CR_CUDA(ctx, cudaMemcpy(recs.data(), cloud->batches, recs.size() * sizeof(cr_batch),

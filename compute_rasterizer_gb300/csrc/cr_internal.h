@@ -40,14 +40,20 @@ struct ViewParams {
     FileRec files[kInlineFiles];
 };
 
-// Scratch words at the head of the ctx scratch buffer.
+// Scratch words at the head of the ctx scratch buffer.  The cull kernel sorts
+// visible batches into two lists sharing one region of `list_cap` words:
+// 10-bit items grow from the front, 20/30-bit items from the back, so the
+// common all-10-bit raster runs in a kernel instance without the wider decode.
 enum : int {
-    kItemCount = 0,   // work items appended by the cull kernel
-    kCursor0 = 1,     // dynamic work cursor, raster / HQS depth pass
-    kCursor1 = 2,     // dynamic work cursor, HQS color pass
-    kCounterWords = 4,
-    kErrWord = 4,     // sticky device error bits (cleared by cr_ctx_check)
-    kScratchHead = 8  // item list starts here
+    kItemCount = 0,   // items in the 10-bit list
+    kCursor0 = 1,     // dynamic work cursor, 10-bit list, raster / HQS depth pass
+    kCursor1 = 2,     // dynamic work cursor, 10-bit list, HQS color pass
+    kItemCount2 = 3,  // items in the 20/30-bit list
+    kCursor2 = 4,     // dynamic work cursor, 20/30-bit list, raster / HQS depth pass
+    kCursor3 = 5,     // dynamic work cursor, 20/30-bit list, HQS color pass
+    kCounterWords = 6,
+    kErrWord = 7,     // sticky device error bits (cleared by cr_ctx_check)
+    kScratchHead = 8  // item lists start here
 };
 
 enum Mode : int { kModeRaster = 0, kModeHqsDepth = 1, kModeHqsColor = 2 };
@@ -62,7 +68,8 @@ struct BatchedLaunch {
     uint64_t* fb;          // u64 framebuffer (raster)
     uint32_t* depth;       // HQS depth
     uint64_t* accum;       // HQS accumulators
-    uint32_t* scratch;     // counters + item list
+    uint32_t* scratch;     // counters + item lists
+    int64_t list_cap;      // words of the item-list region (batch records dispatched)
     int32_t quirks;
     int32_t payload;
     int32_t mode;
@@ -91,5 +98,19 @@ int batched_blocks_per_sm(int mode, int payload, int block);
 // Per-view uniforms from double matrices and per-file boxMin (cr_api.cpp).
 cr_status view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
                           int32_t culling, ViewParams* out);
+
+// Read-only view of a LAS-derived cloud's device layout (cr_api.cpp).
+struct CloudInfo {
+    const cr_batch* batches;
+    const uint32_t* lo;
+    const uint32_t* md;
+    const uint32_t* hi;
+    const uint32_t* rgba;
+    int64_t n, nb, capacity;
+    int32_t nfiles;
+    const double* box_min;  // 3 * nfiles
+};
+bool cloud_info(const cr_cloud* cloud, CloudInfo* out);
+int default_quirks_for(int32_t method);
 
 }  // namespace cr

@@ -27,110 +27,11 @@
 #include <cstdint>
 
 #include "cr_internal.h"
+#include "cr_device.cuh"
 
 namespace cr {
 
 namespace {
-
-constexpr uint32_t kFull = 0xFFFFFFFFu;
-constexpr uint32_t kNoPixel = 0xFFFFFFFFu;
-
-__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
-
-// float(x) for x < 2^23, exact: the bit pattern 2^23 + x minus 2^23.
-__device__ __forceinline__ float small_u2f(uint32_t x) {
-    return __fsub_rn(__uint_as_float(x | 0x4B000000u), 8388608.0f);
-}
-// int(f) for 0 <= f < 2^22 (truncation): add 2^23 rounding toward zero.
-__device__ __forceinline__ int32_t small_f2i(float f) {
-    return __float_as_int(__fadd_rz(f, 8388608.0f)) - 0x4B000000;
-}
-
-__device__ __forceinline__ uint4 ld_stream(const uint4* p) {
-    uint4 r;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-                 : "l"(p));
-    return r;
-}
-
-__device__ __forceinline__ uint32_t lane_id() {
-    uint32_t l;
-    asm("mov.u32 %0, %%laneid;" : "=r"(l));
-    return l;
-}
-
-__device__ __forceinline__ uint32_t u4get(const uint4& v, int j) {
-    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
-}
-
-// ---- per-batch math (render.cs:130-231), no contraction --------------------
-
-__device__ bool intersects_frustum(const float* pl, float mnx, float mny, float mnz, float mxx,
-                                   float mxy, float mxz) {
-#pragma unroll 1
-    for (int i = 0; i < 6; i++) {
-        float nx = pl[4 * i + 0], ny = pl[4 * i + 1], nz = pl[4 * i + 2], c = pl[4 * i + 3];
-        float vx = nx > 0.0f ? mxx : mnx;
-        float vy = ny > 0.0f ? mxy : mny;
-        float vz = nz > 0.0f ? mxz : mnz;
-        float d = fadd(fadd(fadd(fmul(nx, vx), fmul(ny, vy)), fmul(nz, vz)), c);
-        if (d < 0.0f) return false;
-    }
-    return true;
-}
-
-__device__ void mat4_vec4(const float* m, const float v[4], float o[4]) {
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        float s = fmul(m[r], v[0]);
-        s = fadd(s, fmul(m[4 + r], v[1]));
-        s = fadd(s, fmul(m[8 + r], v[2]));
-        s = fadd(s, fmul(m[12 + r], v[3]));
-        o[r] = s;
-    }
-}
-
-__device__ int precision_level(const float* P, const float* VW, int32_t W, int32_t H, float mnx,
-                               float mny, float mnz, float mxx, float mxy, float mxz) {
-    float c[4] = {__fdiv_rn(fadd(mnx, mxx), 2.0f), __fdiv_rn(fadd(mny, mxy), 2.0f),
-                  __fdiv_rn(fadd(mnz, mxz), 2.0f), 1.0f};
-    float dx = fsub(mnx, mxx), dy = fsub(mny, mxy), dz = fsub(mnz, mxz);
-    float radius = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
-    float vc[4], ve[4], pc[4], pe[4];
-    mat4_vec4(VW, c, vc);
-    ve[0] = fadd(vc[0], radius);
-    ve[1] = fadd(vc[1], 0.0f);
-    ve[2] = fadd(vc[2], 0.0f);
-    ve[3] = fadd(vc[3], 0.0f);
-    mat4_vec4(P, vc, pc);
-    mat4_vec4(P, ve, pe);
-    // render.cs:210-211 `xy / w`: one correctly rounded reciprocal per vector
-    const float rc = __frcp_rn(pc[3]), re = __frcp_rn(pe[3]);
-    float pcx = fmul(pc[0], rc), pcy = fmul(pc[1], rc);
-    float pex = fmul(pe[0], re), pey = fmul(pe[1], re);
-    float Wf = (float)W, Hf = (float)H;
-    float scx = __fdiv_rn(fmul(Wf, fadd(pcx, 1.0f)), 2.0f);
-    float scy = __fdiv_rn(fmul(Hf, fadd(pcy, 1.0f)), 2.0f);
-    float sex = __fdiv_rn(fmul(Wf, fadd(pex, 1.0f)), 2.0f);
-    float sey = __fdiv_rn(fmul(Hf, fadd(pey, 1.0f)), 2.0f);
-    float ex = fsub(sex, scx), ey = fsub(sey, scy);
-    float px = __fsqrt_rn(fadd(fmul(ex, ex), fmul(ey, ey)));
-    if (px < 100.0f) return 4;
-    if (px < 200.0f) return 3;
-    if (px < 500.0f) return 2;
-    if (px < 10000.0f) return 1;
-    return 0;
-}
-
-__device__ __forceinline__ int64_t points_in_batch(int32_t num_points, int32_t quirks) {
-    int64_t n = num_points;
-    if (quirks & CR_QUIRK_INCLUSIVE_END) n += 1;
-    if (n > kPointsPerBatch) n = kPointsPerBatch;
-    return n < 0 ? 0 : n;
-}
 
 // ---- cull + level: one thread per batch record -----------------------------
 
@@ -161,110 +62,30 @@ __global__ void __launch_bounds__(256) k_cull(ViewParams vp, const cr_batch* __r
             }
         }
     }
-    uint32_t m = __ballot_sync(kFull, keep);
-    if (m) {
-        uint32_t lane = lane_id();
-        uint32_t leader = __ffs(m) - 1;
+    // 10-bit items to the front of the list region, 20/30-bit items to the back
+    const bool front = keep && (item >> 29) >= 2u;
+    const bool back = keep && !front;
+    const uint32_t lane = lane_id();
+    const uint32_t below = (1u << lane) - 1u;
+    const uint32_t mf = __ballot_sync(kFull, front);
+    if (mf) {
+        const uint32_t leader = __ffs(mf) - 1;
         uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&scratch[kItemCount], __popc(m));
+        if (lane == leader) base = atomicAdd(&scratch[kItemCount], __popc(mf));
         base = __shfl_sync(kFull, base, leader);
-        if (keep) scratch[kScratchHead + base + __popc(m & ((1u << lane) - 1u))] = item;
+        if (front) scratch[kScratchHead + base + __popc(mf & below)] = item;
+    }
+    const uint32_t mb = __ballot_sync(kFull, back);
+    if (mb) {
+        const uint32_t leader = __ffs(mb) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&scratch[kItemCount2], __popc(mb));
+        base = __shfl_sync(kFull, base, leader);
+        if (back) scratch[kScratchHead + nb - 1 - (int64_t)(base + __popc(mb & below))] = item;
     }
 }
 
 // ---- batched raster / HQS body ---------------------------------------------
-
-struct BatchCtx {
-    float mnx, mny, mnz;
-    float sx, sy, sz;
-    float T0, T1, T3, T4, T5, T7, T8, T9, T11, T12, T13, T15;
-    float Wf, Hf;
-    int32_t W;
-};
-
-// Early-z reads of the framebuffer go through L1 and may return a stale copy
-// of a word; within a frame every word only decreases, so a stale value is
-// never below the current one: a point it rejects is rejected by the current
-// value too, and a point it passes goes on to the atomic, which decides.
-__device__ __forceinline__ unsigned long long ld_cached_u64(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ uint32_t ld_cached_u32(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-
-// Per-CTA early-z cache in shared memory: a direct-mapped table (Fibonacci
-// hash of the pixel id) of words `depth << 32 | pixel`.  Every depth stored is
-// one this CTA submitted to, or read from, the framebuffer during the frame, so
-// it is never below the pixel's final minimum depth: a point deeper than the
-// cached depth of its pixel cannot win and is dropped without touching global
-// memory.  Entries are single 64-bit words, so a racing writer replaces an
-// entry but never tears one; the table starts empty (pixel 0xFFFFFFFF).
-constexpr int kZCacheBits = 11;
-constexpr int kZCacheSlots = 1 << kZCacheBits;
-
-__device__ __forceinline__ uint32_t zslot(int32_t pix) {
-    return ((uint32_t)pix * 2654435761u) >> (32 - kZCacheBits);
-}
-
-// Writes one point's contribution.  All 32 lanes of the warp call run()
-// together (inactive lanes with ok = false).  Points that survive the early-z
-// test are merged per pixel inside the warp (__match_any_sync, then a min or
-// sum reduction over the peers), and one leader per pixel issues the atomic.
-template <int MODE>
-struct Emit;
-
-// Leader side of the raster / depth passes: submit `key` for `pix` and record
-// the pixel's new upper bound in the cache.  On a cache miss the framebuffer
-// word is read first (a possibly stale L1 copy, which is still an upper bound)
-// so that a point behind the stored minimum issues no atomic.
-template <typename T>
-__device__ __forceinline__ void submit_min(T* gslot, unsigned long long* zc, uint32_t slot,
-                                           int32_t pix, T key, uint32_t depth_of_key);
-
-template <>
-__device__ __forceinline__ void submit_min<unsigned long long>(unsigned long long* g,
-                                                               unsigned long long* zc,
-                                                               uint32_t slot, int32_t pix,
-                                                               unsigned long long key,
-                                                               uint32_t kd) {
-    const unsigned long long e = zc[slot];
-    uint32_t bound = kd;
-    if ((uint32_t)e == (uint32_t)pix) {
-        atomicMin(g, key);
-    } else {
-        const unsigned long long cur = ld_cached_u64(g);
-        if (key < cur) atomicMin(g, key);
-        else bound = (uint32_t)(cur >> 32);
-    }
-    zc[slot] = ((unsigned long long)bound << 32) | (uint32_t)pix;
-}
-
-template <>
-__device__ __forceinline__ void submit_min<uint32_t>(uint32_t* g, unsigned long long* zc,
-                                                     uint32_t slot, int32_t pix, uint32_t key,
-                                                     uint32_t kd) {
-    const unsigned long long e = zc[slot];
-    uint32_t bound = kd;
-    if ((uint32_t)e == (uint32_t)pix) {
-        atomicMin(g, key);
-    } else {
-        const uint32_t cur = ld_cached_u32(g);
-        if (key < cur) atomicMin(g, key);
-        else bound = cur;
-    }
-    zc[slot] = ((unsigned long long)bound << 32) | (uint32_t)pix;
-}
-
-__device__ __forceinline__ bool zcache_rejects(const unsigned long long* zc, uint32_t slot,
-                                               int32_t pix, uint32_t wbits) {
-    const unsigned long long e = zc[slot];
-    return (uint32_t)e == (uint32_t)pix && wbits > (uint32_t)(e >> 32);
-}
 
 // The raster and depth passes merge same-pixel candidates through the CTA's
 // z-cache rather than with __match_any_sync: a warp vote skips the atomic path
@@ -277,13 +98,13 @@ struct Emit<kModeRaster> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long* zc,
                                                bool ok, int32_t pix, uint32_t wbits,
                                                uint32_t payload, uint32_t) {
-        const uint32_t slot = zslot(pix);
+        const uint32_t slot = zslot((uint32_t)pix);
         // render.cs:423-424 early depth test, against the CTA's cache
-        const bool cand = ok && !zcache_rejects(zc, slot, pix, wbits);
+        const bool cand = ok && !zcache_rejects(zc, slot, (uint32_t)pix, wbits);
         if (__any_sync(kFull, cand) && cand)
             submit_min<unsigned long long>(reinterpret_cast<unsigned long long*>(bl.fb) + pix, zc,
-                                           slot, pix, ((unsigned long long)wbits << 32) | payload,
-                                           wbits);
+                                           slot, (uint32_t)pix,
+                                           ((unsigned long long)wbits << 32) | payload, wbits);
     }
 };
 
@@ -292,11 +113,11 @@ struct Emit<kModeHqsDepth> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long* zc,
                                                bool ok, int32_t pix, uint32_t wbits, uint32_t,
                                                uint32_t) {
-        const uint32_t slot = zslot(pix);
+        const uint32_t slot = zslot((uint32_t)pix);
         // hqs/depth.cs:375-379
-        const bool cand = ok && !zcache_rejects(zc, slot, pix, wbits);
+        const bool cand = ok && !zcache_rejects(zc, slot, (uint32_t)pix, wbits);
         if (__any_sync(kFull, cand) && cand)
-            submit_min<uint32_t>(bl.depth + pix, zc, slot, pix, wbits, wbits);
+            submit_min<uint32_t>(bl.depth + pix, zc, slot, (uint32_t)pix, wbits, wbits);
     }
 };
 
@@ -332,25 +153,6 @@ struct Emit<kModeHqsColor> {
         }
     }
 };
-
-// Project a decoded point (render.cs:399-409 under the arithmetic contract).
-__device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, float z, int32_t& pix,
-                                        uint32_t& wbits) {
-    float px = __fmaf_rn(c.T8, z, __fmaf_rn(c.T4, y, __fmaf_rn(c.T0, x, c.T12)));
-    float py = __fmaf_rn(c.T9, z, __fmaf_rn(c.T5, y, __fmaf_rn(c.T1, x, c.T13)));
-    float pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
-    // render.cs:402 `pos.xyz / pos.w`: one correctly rounded reciprocal of w
-    const float rw = __frcp_rn(pw);
-    float qx = fmul(px, rw), qy = fmul(py, rw);
-    // render.cs:404 written positively, so a NaN position is outside (the
-    // negated form would keep it and index the framebuffer with garbage)
-    bool in = pw > 0.0f && qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f;
-    int32_t ix = small_f2i(fmul(__fmaf_rn(qx, 0.5f, 0.5f), c.Wf));
-    int32_t iy = small_f2i(fmul(__fmaf_rn(qy, 0.5f, 0.5f), c.Hf));
-    pix = ix + iy * c.W;
-    wbits = __float_as_uint(pw);
-    return in;
-}
 
 // LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0).
 // Points [first, first + count) are read as 128-bit vectors starting at the
@@ -423,12 +225,18 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
     }
 }
 
-template <int MODE, int PAYLOAD, int BLOCK>
+// LIST 0: the 10-bit items (front of the list region), LIST 1: the 20/30-bit
+// items (back of the region).  Each list runs in its own instance, so the
+// common 10-bit instance carries no wider decode state (fewer registers).
+template <int MODE, int PAYLOAD, int BLOCK, int LIST>
 __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch bl) {
     __shared__ uint32_t s_item[2];
     __shared__ unsigned long long s_zc[MODE == kModeHqsColor ? 1 : kZCacheSlots];
-    uint32_t* cursor = bl.scratch + (MODE == kModeHqsColor ? kCursor1 : kCursor0);
-    const uint32_t nitems = *reinterpret_cast<volatile uint32_t*>(bl.scratch + kItemCount);
+    uint32_t* cursor = bl.scratch + (LIST == 0 ? (MODE == kModeHqsColor ? kCursor1 : kCursor0)
+                                               : (MODE == kModeHqsColor ? kCursor3 : kCursor2));
+    const uint32_t nitems =
+        *reinterpret_cast<volatile uint32_t*>(bl.scratch + (LIST == 0 ? kItemCount : kItemCount2));
+    if (nitems == 0) return;
     if (MODE != kModeHqsColor)
         for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
     if (threadIdx.x == 0) s_item[0] = atomicAdd(cursor, 1u);
@@ -438,7 +246,8 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
         const uint32_t wi = s_item[buf];
         if (wi >= nitems) break;
         if (threadIdx.x == 0) s_item[buf ^ 1] = atomicAdd(cursor, 1u);
-        const uint32_t item = bl.scratch[kScratchHead + wi];
+        const uint32_t item =
+            bl.scratch[kScratchHead + (LIST == 0 ? (int64_t)wi : bl.list_cap - 1 - (int64_t)wi)];
         const uint32_t b = item & 0x1FFFFFFFu;
         const int level = (int)(item >> 29);
 
@@ -462,7 +271,7 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
         c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
         c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
         const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-        if (level >= 2) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
+        if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
         else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, first, count, l0_x12);
         else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, first, count, l0_x12);
         __syncthreads();
@@ -631,14 +440,22 @@ int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb, int64
     return launch_status();
 }
 
+template <int MODE, int PAYLOAD, int LIST>
+static void launch_list(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
+                        cudaStream_t s) {
+    switch (block) {
+        case 128: k_batched<MODE, PAYLOAD, 128, LIST><<<grid, 128, 0, s>>>(vp, bl); break;
+        case 512: k_batched<MODE, PAYLOAD, 512, LIST><<<grid, 512, 0, s>>>(vp, bl); break;
+        default: k_batched<MODE, PAYLOAD, 256, LIST><<<grid, 256, 0, s>>>(vp, bl); break;
+    }
+}
+
+// The 10-bit list, then the (usually short) 20/30-bit list.
 template <int MODE, int PAYLOAD>
 static void launch_batched_t(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
                              cudaStream_t s) {
-    switch (block) {
-        case 128: k_batched<MODE, PAYLOAD, 128><<<grid, 128, 0, s>>>(vp, bl); break;
-        case 512: k_batched<MODE, PAYLOAD, 512><<<grid, 512, 0, s>>>(vp, bl); break;
-        default: k_batched<MODE, PAYLOAD, 256><<<grid, 256, 0, s>>>(vp, bl); break;
-    }
+    launch_list<MODE, PAYLOAD, 0>(vp, bl, block, grid, s);
+    launch_list<MODE, PAYLOAD, 1>(vp, bl, block, grid, s);
 }
 
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid, void* stream) {
@@ -659,9 +476,9 @@ static int occupancy_t(int block) {
     int n = 0;
     cudaError_t e;
     switch (block) {
-        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128>, 128, 0); break;
-        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 512>, 512, 0); break;
-        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 256>, 256, 0); break;
+        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0>, 128, 0); break;
+        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 512, 0>, 512, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 256, 0>, 256, 0); break;
     }
     return e == cudaSuccess ? n : 1;
 }

@@ -95,6 +95,7 @@ extern "C" cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_
     bl.capacity = stream_words;
     bl.fb = d_fb;
     bl.scratch = scratch;
+    bl.list_cap = nb;
     bl.quirks = quirks;
     bl.payload = p->payload;
     bl.mode = cr::kModeRaster;

@@ -1,0 +1,81 @@
+"""The benchmark workloads: synthetic clouds and cameras.
+
+Seeded, so every run renders the same frames:
+  * terrain_frame      1 view, the reference's zoom-to-cloud pose
+                       (src/main.cpp:251-270), 1920x1080.
+  * flight_path        5 poses along a seeded flight over a terrain, 2560x1440.
+  * multiview_64       16 stereo pairs at 1440x1600 per eye (IPD 0.064 m,
+                       parallel eye axes) flying over the cloud + 32 random
+                       orbit poses at 512x512.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib as L
+from . import synth
+
+
+def _perspective(fovy, w, h, znear=0.1, zfar=200000.0):
+    return synth.perspective(fovy, w / h, znear, zfar)
+
+
+def terrain_frame(box_min, box_max, width=1920, height=1080):
+    yaw, pitch, radius, target = synth.zoom_to_cloud(box_min, box_max)
+    return synth.orbit_view(yaw, pitch, radius, target), _perspective(60.0, width, height), width, height
+
+
+def flight_path(box_min, box_max, n=5, seed=2, width=2560, height=1440):
+    """Poses along a seeded flight: orbit cameras drifting over the cloud."""
+    rng = np.random.default_rng(seed)
+    bmin, bmax = np.asarray(box_min, float), np.asarray(box_max, float)
+    size = bmax - bmin
+    cams = []
+    start = bmin + size * np.array([0.2, 0.2, 0.5])
+    end = bmin + size * np.array([0.8, 0.7, 0.5])
+    for i in range(n):
+        t = i / max(1, n - 1)
+        target = start + t * (end - start)
+        yaw = 0.6 + 1.5 * t + rng.uniform(-0.2, 0.2)
+        pitch = -0.45 - 0.3 * rng.uniform()
+        radius = float(np.linalg.norm(size[:2])) * (0.08 + 0.25 * rng.uniform())
+        cams.append((synth.orbit_view(yaw, pitch, radius, target), _perspective(60.0, width, height),
+                     width, height))
+    return cams
+
+
+def _look_dir(yaw, pitch):
+    return np.array([math.cos(pitch) * math.cos(yaw), math.cos(pitch) * math.sin(yaw), math.sin(pitch)])
+
+
+def multiview_64(box_min, box_max, seed=4, ipd=0.064):
+    """16 stereo pairs (1440x1600 per eye) + 32 random poses (512x512)."""
+    rng = np.random.default_rng(seed)
+    bmin, bmax = np.asarray(box_min, float), np.asarray(box_max, float)
+    size = bmax - bmin
+    up = np.array([0.0, 0.0, 1.0])
+    cams = []
+    for _ in range(16):
+        centre = bmin + size * np.array([rng.uniform(0.15, 0.85), rng.uniform(0.15, 0.85), 1.0])
+        centre[2] = bmax[2] + rng.uniform(20.0, 150.0)
+        d = _look_dir(rng.uniform(-math.pi, math.pi), rng.uniform(-0.6, -0.15))
+        right = np.cross(d, up)
+        right /= np.linalg.norm(right)
+        for side in (-0.5, 0.5):
+            eye = centre + side * ipd * right
+            cams.append((synth.look_at(eye, eye + d, up), _perspective(90.0, 1440, 1600), 1440, 1600))
+    yaw0, pitch0, radius0, target0 = synth.zoom_to_cloud(bmin, bmax)
+    for _ in range(32):
+        target = bmin + size * np.array([rng.uniform(0.1, 0.9), rng.uniform(0.1, 0.9), 0.5])
+        view = synth.orbit_view(rng.uniform(-math.pi, math.pi), rng.uniform(-1.3, -0.25),
+                                radius0 * rng.uniform(0.1, 1.0), target)
+        cams.append((view, _perspective(60.0, 512, 512), 512, 512))
+    return cams
+
+
+def multiview_cloud_params(seed=4, extent=4500.0):
+    """Terrain plus 2000 boxes (10-60 m tall, 20k points on their faces)."""
+    return synth.synth_params(L.SYNTH_TERRAIN_BOXES, extent, seed, num_boxes=2000,
+                              points_per_box=20000, box_min_height=10.0, box_max_height=60.0)

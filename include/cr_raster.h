@@ -193,6 +193,49 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
 cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params* params,
                      cr_fb* fb, void* stream);
 
+/* ---- many views of one cloud in one persistent launch ------------------------
+ * The reference renders two eyes from one fetch of each point
+ * (compute_loop_las_hqs_vr/depth.cs:374-412).  A multi-view plan generalises
+ * that to any number of views of uneven size, in groups of up to
+ * CR_MV_MAX_GROUP views: each work item is (batch, view group); a CTA fetches
+ * the batch's points once and splats them into every view of the group whose
+ * frustum the batch AABB intersects, each view at its own precision level, so
+ * every view's framebuffer is bit-identical to a cr_render of that view alone.
+ * The plan owns one framebuffer (u64 words + RGBA8 image) per view.  Its
+ * frame (uniform upload, counter reset, cull, raster, resolve + re-clear) can
+ * be captured once into a CUDA graph and replayed. */
+#define CR_MV_MAX_GROUP 8
+typedef struct cr_mv cr_mv;
+/* params: method loop_las or loop_las_prefetch; payload, quirks, culling,
+ * resolve, clear_after, clear_value as for cr_render; views_per_group 1..8
+ * (0 = 8); block_threads 64/128/256 (0 = 128); ctas_per_sm (0 = occupancy). */
+cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t num_views,
+                       const int32_t* widths, const int32_t* heights,
+                       const cr_render_params* params, cr_mv** out);
+cr_status cr_mv_destroy(cr_mv* mv);
+const char* cr_mv_last_error(const cr_mv* mv);
+/* Replaces the launch parameters (drops a captured graph). */
+cr_status cr_mv_set_params(cr_mv* mv, const cr_render_params* params);
+cr_status cr_mv_get_params(const cr_mv* mv, cr_render_params* out);
+/* Sets all num_views cameras (sizes must match the plan).  Waits for the
+ * previous frame's uniform upload before overwriting the staging copy. */
+cr_status cr_mv_set_views(cr_mv* mv, const cr_view* views);
+/* Enqueues one frame on `stream`.  use_graph = 1 captures the frame into a
+ * CUDA graph on the first call and replays it afterwards (needs a stream
+ * other than the legacy default stream). */
+cr_status cr_mv_render(cr_mv* mv, int32_t use_graph, void* stream);
+/* Every view's words = value (the start state of the first frame). */
+cr_status cr_mv_clear(cr_mv* mv, uint64_t value, void* stream);
+/* Device -> host copy of one view's CR_FB_WORDS or CR_FB_IMAGE (caller syncs). */
+cr_status cr_mv_read(cr_mv* mv, int32_t view, int32_t what, void* host_dst, int64_t bytes,
+                     void* stream);
+/* Autotuner: times `frames` frames of every block size {64, 128, 256} x views
+ * per group {1, 2, 4, 8} (points per thread 160, 80, 40) for the current
+ * views, keeps the fastest in the plan, returns it in *best and a JSON report
+ * of every configuration's milliseconds in `report` (may be NULL). */
+cr_status cr_mv_autotune(cr_mv* mv, int32_t frames, void* stream, cr_render_params* best,
+                         char* report, int32_t report_bytes);
+
 /* ---- rasterizing without allocating ------------------------------------------
  * No counterpart in the reference (its Methods own GL buffers created at
  * start-up).  For callers that must not allocate device memory while they

@@ -1,0 +1,128 @@
+"""Multi-view plans: every view's framebuffer and image equal a cr_render of
+that view alone, bit for bit, for every group width, block size and payload,
+with and without CUDA-graph replay; the oracle agrees on sampled views."""
+import numpy as np
+import pytest
+
+from compute_rasterizer_gb300 import _lib as L
+from compute_rasterizer_gb300 import default_params, make_view, synth
+from compute_rasterizer_gb300.multiview import MultiView
+from helpers import QUIRKS, camera_views, encoded, first_diff, gpu_raw, oracle_frame
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene(ctx):
+    cl = encoded(n=62674, extent=200.0, seed=7)
+    cloud = ctx.cloud_from_arrays(cl["batches"], cl["lo"], cl["md"], cl["hi"], cl["rgba"],
+                                  cl["box_min"])
+    base = camera_views(cl["box_min"], cl["box_max"], cl["batches"])
+    rng = np.random.default_rng(5)
+    target = (cl["box_min"] + cl["box_max"]) / 2
+    views = list(base.values())
+    for _ in range(7):
+        views.append(synth.orbit_view(rng.uniform(-3, 3), rng.uniform(-1.3, -0.2),
+                                      rng.uniform(20, 400), target + rng.uniform(-60, 60, 3)))
+    sizes = [(320, 240), (64, 48), (200, 150), (96, 96), (333, 111), (128, 256), (40, 30),
+             (256, 256), (150, 100), (77, 55), (300, 200)]
+    cams = []
+    for v, (w, h) in zip(views, sizes):
+        cams.append((v, synth.perspective(60.0, w / h, 0.1, 200000.0), w, h))
+    return cl, cloud, cams
+
+
+def single_view(ctx, cloud, cam, method, payload):
+    fb, params = gpu_raw(ctx, cloud, cam, method, payload)
+    words = fb.read(L.FB_WORDS)
+    ctx.resolve(cloud, params, fb)
+    return words, fb.read(L.FB_IMAGE)
+
+
+@pytest.mark.parametrize("group,block", [(1, 128), (3, 64), (8, 128), (8, 256), (5, 128)])
+@pytest.mark.parametrize("method,payload", [(L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX),
+                                            (L.METHOD_LOOP_LAS_PREFETCH, L.PAYLOAD_COLOR)])
+def test_multiview_equals_single_views(ctx, scene, group, block, method, payload):
+    cl, cloud, cams = scene
+    params = default_params(method, payload=payload, views_per_group=group, block_threads=block,
+                            resolve=0, clear_after=0)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    mv.clear()
+    mv.render()
+    ctx.sync()
+    words = [mv.read(i, L.FB_WORDS) for i in range(len(cams))]
+    params.resolve = 1
+    mv.set_params(params)
+    mv.clear()
+    mv.render()
+    ctx.sync()
+    for i, cam in enumerate(cams):
+        want_w, want_img = single_view(ctx, cloud, cam, method, payload)
+        assert np.array_equal(words[i], want_w), (i, first_diff(words[i], want_w))
+        img = mv.read(i, L.FB_IMAGE)
+        assert np.array_equal(img, want_img), (i, first_diff(img, want_img))
+    mv.close()
+
+
+def test_multiview_matches_oracle_on_sampled_views(ctx, scene):
+    cl, cloud, cams = scene
+    params = default_params(L.METHOD_LOOP_LAS, views_per_group=8, resolve=0, clear_after=0)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    mv.clear()
+    mv.render()
+    ctx.sync()
+    for i in (0, 1, 2, 5, 9):
+        fr = oracle_frame(cams[i], cl["box_min"][None], QUIRKS[L.METHOD_LOOP_LAS])
+        want = O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+        got = mv.read(i, L.FB_WORDS)
+        assert np.array_equal(got, want), (i, first_diff(got, want))
+    mv.close()
+
+
+def test_multiview_graph_replay_and_clear(ctx, scene):
+    import torch
+    cl, cloud, cams = scene
+    params = default_params(L.METHOD_LOOP_LAS, payload=L.PAYLOAD_COLOR, views_per_group=4)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    s = torch.cuda.Stream()
+    mv.clear(stream=s.cuda_stream)
+    for _ in range(3):  # capture on the first call, replay after
+        mv.render(use_graph=True, stream=s.cuda_stream)
+    ctx.sync(s.cuda_stream)
+    for i, cam in enumerate(cams):
+        _, want_img = single_view(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+        assert np.array_equal(mv.read(i, L.FB_IMAGE, s.cuda_stream), want_img), i
+        # resolve re-cleared every word, guard tail included
+        assert (mv.read(i, L.FB_WORDS, s.cuda_stream) == L.DEFAULT_CLEAR).all(), i
+    # new cameras reach the captured graph through the staging copy
+    mv.set_views([make_view(cams[(i + 1) % len(cams)][0], cams[i][1], cams[i][2], cams[i][3])
+                  for i in range(len(cams))])
+    mv.render(use_graph=True, stream=s.cuda_stream)
+    ctx.sync(s.cuda_stream)
+    for i in (0, 4):
+        cam = (cams[(i + 1) % len(cams)][0], cams[i][1], cams[i][2], cams[i][3])
+        _, want_img = single_view(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+        assert np.array_equal(mv.read(i, L.FB_IMAGE, s.cuda_stream), want_img), i
+    mv.close()
+
+
+def test_autotune_keeps_output_identical(ctx, scene):
+    cl, cloud, cams = scene
+    params = default_params(L.METHOD_LOOP_LAS, resolve=0, clear_after=0)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    mv.clear()
+    best, report = mv.autotune(frames=2)
+    assert best.block_threads in (64, 128, 256) and best.views_per_group in (1, 2, 4, 8)
+    assert len(report) == 12 and all(v > 0 for v in report.values())
+    mv.clear()
+    mv.render()
+    ctx.sync()
+    for i in (0, 3, 7):
+        want, _ = single_view(ctx, cloud, cams[i], L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX)
+        assert np.array_equal(mv.read(i, L.FB_WORDS), want), i
+    mv.close()

@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--serving", default="quick", choices=["quick", "full", "off"])
     return ap.parse_args()
 
 
@@ -316,6 +317,11 @@ def main():
             out["extras"]["multiview_64"] = multiview_64(ctx, sh, args.steps, payload)
         except Exception as exc:  # the headline line is printed regardless
             out["extras"]["multiview_64"] = {"error": repr(exc)}
+        if args.serving != "off":
+            try:
+                out["extras"]["serving"] = serving(ctx, sh, args, payload)
+            except Exception as exc:
+                out["extras"]["serving"] = {"error": repr(exc)}
     if not args.no_e2e:
         out["e2e"] = e2e(ctx, cloud, cv, params, fb, sh, n, args, bmin)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -410,6 +416,118 @@ def multiview_64(ctx, sh, steps, payload):
     for f in fbs:
         f.close()
     cloud.close()
+    return out
+
+
+def serving(ctx, sh, args, payload):
+    """8 resident terrains (10-500 M points), requests with Poisson arrivals,
+    clouds drawn Zipf(1.1), random orbit cameras at five resolutions, an 8 GiB
+    framebuffer pool.  Both arms run the same replay through the frame server:
+    batched (continuous batching into multi-view launches) and plain (one
+    single-view render per request).  Every request's image is copied back to
+    pinned host memory inside its latency."""
+    import torch
+
+    import compute_rasterizer_gb300 as cr
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import synth, workloads
+    from compute_rasterizer_gb300.serve import Server, latency_summary
+
+    clouds, boxes = [], []
+    for i, m in enumerate(workloads.SERVING_CLOUD_MPOINTS):
+        n = m * 1_000_000
+        c, hdr = synth.build_cloud_device(ctx, workloads.serving_cloud_params(i, n), n, sh)
+        clouds.append(c)
+        boxes.append((np.array(hdr.min[:]), np.array(hdr.max[:])))
+    ctx.sync(sh)
+    # a ring of pinned host memory for the returned images; the pool bounds the
+    # bytes in flight (images are a third of each request's pool bytes)
+    ring_bytes = 4 << 30
+    ring = torch.empty(ring_bytes // 4, dtype=torch.int32, pin_memory=True)
+    ring_np = ring.numpy().view(np.uint32)
+    cursor = [0]
+
+    def host_slot(words):
+        if cursor[0] + words > ring_np.size:
+            cursor[0] = 0
+        a = ring_np[cursor[0]:cursor[0] + words]
+        cursor[0] += words
+        return a
+
+    def make_requests(cams):
+        return [Server.request(c, cr.make_view(v, p, w, h), host_slot(w * h), user_tag=i)
+                for i, (c, v, p, w, h) in enumerate(cams)]
+
+    def server(plain):
+        srv = Server(ctx, pool_bytes=8 << 30, max_batch_views=64, max_inflight=2,
+                     plain_launches=plain, payload=payload)
+        for c in clouds:
+            srv.add_cloud(c)
+        return srv
+
+    arms = {"batched": server(False), "plain": server(True)}
+    out = {"clouds_mpoints": list(workloads.SERVING_CLOUD_MPOINTS),
+           "resolutions": [f"{w}x{h}" for w, h in workloads.SERVING_RESOLUTIONS],
+           "zipf_s": 1.1, "pool_bytes": 8 << 30, "max_batch_views": 64, "max_inflight": 2,
+           "payload": "color" if payload == L.PAYLOAD_COLOR else "index",
+           "latency": "arrival -> image in pinned host memory (server clock)"}
+    # warm-up
+    arr, cams = workloads.serving_requests(boxes, 64, 1e5, seed=99)
+    for srv in arms.values():
+        srv.replay(make_requests(cams), arr)
+
+    # capacity: a burst of requests all arriving at t = 0
+    nb = 2000 if args.serving == "full" else 800
+    arr, cams = workloads.serving_requests(boxes, nb, 1e9, seed=7)
+    cap = {}
+    for name, srv in arms.items():
+        done = srv.replay(make_requests(cams), np.zeros(nb))
+        cap[name] = latency_summary(done)
+    out["capacity_req_per_s"] = {k: round(v["served_req_per_s"], 1) for k, v in cap.items()}
+    out["capacity_speedup_vs_plain"] = round(cap["batched"]["served_req_per_s"]
+                                             / cap["plain"]["served_req_per_s"], 3)
+    out["capacity_mean_batch_views"] = round(cap["batched"]["mean_batch_views"], 2)
+
+    rates = ([100, 250, 500, 1000, 2000, 3000, 4000, 5000] if args.serving == "full"
+             else [500, 2000, 5000])
+    seconds = 2.0 if args.serving == "full" else 1.0
+    sweep = []
+    for k, rate in enumerate(rates):
+        n = int(max(200, min(rate * seconds, 10000)))
+        arr, cams = workloads.serving_requests(boxes, n, float(rate), seed=20 + k)
+        row = {"rate_req_per_s": rate, "requests": n}
+        for name, srv in arms.items():
+            s = latency_summary(srv.replay(make_requests(cams), arr))
+            row[name] = {key: (round(v, 3) if isinstance(v, float) else v) for key, v in s.items()}
+        row["p99_ratio_plain_over_batched"] = round(row["plain"]["p99_ms"] / row["batched"]["p99_ms"], 3)
+        sweep.append(row)
+    out["sweep"] = sweep
+    for name, srv in arms.items():
+        st = srv.stats()
+        out[f"{name}_stats"] = {k: st[k] for k in ("launches", "views_launched", "max_views_in_launch",
+                                                   "rejected", "failed", "pool_peak_bytes")}
+
+    # bit-exact: a mixed burst against each request rendered alone
+    arr, cams = workloads.serving_requests(boxes, 64, 1e9, seed=123)
+    imgs = [np.zeros(w * h, np.uint32) for (_, _, _, w, h) in cams]
+    reqs = [Server.request(c, cr.make_view(v, p, w, h), imgs[i], user_tag=i)
+            for i, (c, v, p, w, h) in enumerate(cams)]
+    done = arms["batched"].replay(reqs, np.zeros(len(reqs)))
+    params = cr.default_params(L.METHOD_LOOP_LAS, payload=payload, resolve=1, clear_after=0)
+    same = bool((done["status"] == L.OK).all())
+    for i, (c, v, p, w, h) in enumerate(cams):
+        fb = ctx.framebuffer(w, h)
+        fb.clear(stream=sh)
+        ctx.render(clouds[c], cr.make_view(v, p, w, h), params, fb, sh)
+        same = same and np.array_equal(fb.read(L.FB_IMAGE, sh), imgs[i])
+        fb.close()
+    out["bit_exact_alone_vs_mix"] = same
+    out["bit_exact_checked"] = {"requests": len(cams),
+                                "mean_batch_views": round(float(done["batch_views"].mean()), 2)}
+    for srv in arms.values():
+        srv.close()
+    for c in clouds:
+        c.close()
     return out
 
 

@@ -1,4 +1,4 @@
-"""ctypes binding of include/cr_raster.h and include/cr_synth.h.
+"""ctypes binding of include/cr_raster.h, include/cr_synth.h and include/cr_serve.h.
 
 The CUDA library is built in-tree (compute_rasterizer_gb300/_build/libcr_raster.so
 by compute_rasterizer_gb300.build).  There is no CPU fallback: loading fails
@@ -80,6 +80,37 @@ class SynthParams(C.Structure):
                 ("origin", C.c_double * 2)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("pool_bytes", C.c_int64), ("max_batch_views", C.c_int32),
+                ("max_inflight", C.c_int32), ("max_queued", C.c_int32),
+                ("plain_launches", C.c_int32), ("method", C.c_int32), ("payload", C.c_int32),
+                ("quirks", C.c_int32), ("frustum_culling", C.c_int32),
+                ("views_per_group", C.c_int32), ("block_threads", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
+
+
+class Request(C.Structure):
+    _fields_ = [("cloud", C.c_int32), ("reserved0", C.c_int32), ("view", View),
+                ("host_image", C.c_void_p), ("user_tag", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("user_tag", C.c_uint64), ("status", C.c_int32),
+                ("batch_views", C.c_int32), ("t_arrival_us", C.c_double),
+                ("t_launch_us", C.c_double), ("t_done_us", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("rejected", C.c_int64), ("completed", C.c_int64),
+                ("failed", C.c_int64), ("launches", C.c_int64), ("views_launched", C.c_int64),
+                ("pool_bytes", C.c_int64), ("pool_used_bytes", C.c_int64),
+                ("pool_peak_bytes", C.c_int64), ("max_views_in_launch", C.c_int32),
+                ("queued", C.c_int32), ("gpu_ms", C.c_double)]
+
+
+SERVE_MAX_POOL_BYTES = 16 << 30
+SERVE_MAX_BATCH_VIEWS = 256
+
 P = C.c_void_p
 I32, I64, U64, DBL, FLT = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_float
 PP = C.POINTER(C.c_void_p)
@@ -148,6 +179,17 @@ _SIGS = {
     "cr_synth_cloud_device": (I32, [P, C.POINTER(SynthParams), I64, P, C.POINTER(LasHeader), P]),
     "cr_synth_uniform_host": (I32, [U64, I64, FLT, P]),
     "cr_synth_uniform_device": (I32, [P, U64, I64, FLT, P, P]),
+    # cr_serve.h
+    "cr_server_create": (I32, [P, C.POINTER(ServerConfig), PP]),
+    "cr_server_destroy": (I32, [P]),
+    "cr_server_last_error": (C.c_char_p, [P]),
+    "cr_server_now_us": (DBL, [P]),
+    "cr_server_add_cloud": (I32, [P, P, C.POINTER(I32)]),
+    "cr_server_submit": (I32, [P, C.POINTER(Request), C.POINTER(U64)]),
+    "cr_server_poll": (I32, [P, C.POINTER(Completion), I32, C.POINTER(I32), I32]),
+    "cr_server_drain": (I32, [P, I32]),
+    "cr_server_replay": (I32, [P, C.POINTER(Request), C.POINTER(DBL), I64, C.POINTER(Completion)]),
+    "cr_server_stats_get": (I32, [P, C.POINTER(ServerStats)]),
 }
 
 EXPORTED = tuple(_SIGS)

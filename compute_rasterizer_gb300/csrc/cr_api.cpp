@@ -234,6 +234,8 @@ bool cr::cloud_info(const cr_cloud* c, CloudInfo* out) {
 
 int cr::default_quirks_for(int32_t method) { return default_quirks(method); }
 
+int cr::ctx_device(const cr_ctx* ctx) { return ctx ? ctx->device : 0; }
+
 cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
                               int32_t culling, ViewParams* vp) {
     if (!view || !box_min || !vp || num_files < 1 || num_files > kInlineFiles)

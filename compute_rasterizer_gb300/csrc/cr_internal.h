@@ -112,5 +112,47 @@ struct CloudInfo {
 };
 bool cloud_info(const cr_cloud* cloud, CloudInfo* out);
 int default_quirks_for(int32_t method);
+int ctx_device(const cr_ctx* ctx);
+
+// ---- multi-view frames (cr_multiview.cu), shared by cr_mv plans and the server
+
+// Per (view, file): the 12 transform entries the projection uses (T0, T1, T3,
+// T4, T5, T7, T8, T9, T11, T12, T13, T15), the frustum planes, view * world.
+struct MVFile {
+    float T[12];
+    float planes[24];
+    float VW[16];
+};
+
+struct MVView {
+    float P[16];
+    int32_t W, H;
+    uint32_t fb_off;   // u64 word offset of the view's framebuffer from MVFrame::fbs
+    uint32_t img_off;  // u32 offset of the view's image from MVFrame::images
+};
+
+// Fills a view's P, W, H and its nfiles per-file records from the double
+// matrices (the single-view uniforms, so each view renders as cr_render would).
+cr_status mv_fill_view(const cr_view* view, const CloudInfo& ci, MVView* out_view,
+                       MVFile* out_files);
+
+// One multi-view frame over device-resident view records.
+struct MVFrame {
+    CloudInfo ci;
+    const MVView* d_views;
+    const MVFile* d_files;
+    int32_t nviews;
+    uint64_t* fbs;
+    uint32_t* images;
+    uint32_t* scratch;       // mv_scratch_words(ci.nb, nviews) words
+    int32_t G, block, ctas_per_sm, quirks, payload, culling, num_sms;
+    int32_t clear_before;    // fill every view's W*H+W+1 words with clear_value first
+    int32_t resolve, clear_after;
+    uint64_t clear_value;
+    int64_t max_words;       // max over the views of W*H+W+1
+};
+int64_t mv_scratch_words(int64_t nb, int64_t nviews);
+// Enqueues counter reset, [fill], cull, raster (both lists), [resolve] on stream.
+cr_status mv_enqueue(const MVFrame& f, void* stream, const char** what);
 
 }  // namespace cr

@@ -27,21 +27,6 @@
 namespace cr {
 namespace {
 
-// Per (view, file): the 12 transform entries the projection uses (T0, T1, T3,
-// T4, T5, T7, T8, T9, T11, T12, T13, T15), the frustum planes, view * world.
-struct MVFile {
-    float T[12];
-    float planes[24];
-    float VW[16];
-};
-
-struct MVView {
-    float P[16];
-    int32_t W, H;
-    uint32_t fb_off;   // word offset of the view's framebuffer
-    uint32_t img_off;  // pixel offset of the view's image
-};
-
 struct MVArgs {
     const MVView* views;
     const MVFile* files;
@@ -338,6 +323,18 @@ __global__ void k_mv_fill(unsigned long long* p, int64_t n, unsigned long long v
         p[i] = v;
 }
 
+// The clear of compute_loop_las.h:288-301 for every view of a frame (grid y =
+// view): W*H+W+1 words each, the guard tail included.
+__global__ void k_mv_fill_views(const MVView* __restrict__ views, unsigned long long* fbs,
+                                unsigned long long v) {
+    const MVView vw = views[blockIdx.y];
+    const int64_t n = (int64_t)vw.W * vw.H + vw.W + 1;
+    unsigned long long* fb = fbs + vw.fb_off;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        fb[i] = v;
+}
+
 // The 10-bit list, then the 20/30-bit list, on one stream.
 template <int PAYLOAD, int LIST>
 void launch_mv_list(const MVArgs& a, int block, int grid, cudaStream_t s) {
@@ -369,7 +366,93 @@ int mv_occupancy_t(int block) {
     return e == cudaSuccess && n > 0 ? n : 1;
 }
 
+int64_t dispatched(const CloudInfo& ci, int quirks) {
+    int64_t nb = ci.nb;
+    if (quirks & CR_QUIRK_DISPATCH_BY_POINTS)
+        nb = std::min<int64_t>(nb, (ci.n + kPointsPerBatch - 1) / kPointsPerBatch);
+    return nb;
+}
+
 }  // namespace
+
+int64_t mv_scratch_words(int64_t nb, int64_t nviews) { return kScratchHead + 4 * nb * nviews + 64; }
+
+cr_status mv_fill_view(const cr_view* view, const CloudInfo& ci, MVView* out_view,
+                       MVFile* out_files) {
+    ViewParams vp;
+    cr_status s = view_params_for(view, ci.box_min, ci.nfiles, 1, &vp);
+    if (s != CR_OK) return s;
+    std::memcpy(out_view->P, vp.P, sizeof(vp.P));
+    out_view->W = view->width;
+    out_view->H = view->height;
+    const int pick[12] = {0, 1, 3, 4, 5, 7, 8, 9, 11, 12, 13, 15};
+    for (int f = 0; f < ci.nfiles; f++) {
+        MVFile& o = out_files[f];
+        const FileRec& r = vp.files[f];
+        for (int k = 0; k < 12; k++) o.T[k] = r.T[pick[k]];
+        std::memcpy(o.planes, r.planes, sizeof(o.planes));
+        std::memcpy(o.VW, r.VW, sizeof(o.VW));
+    }
+    return CR_OK;
+}
+
+cr_status mv_enqueue(const MVFrame& f, void* stream, const char** what) {
+    cudaStream_t st = (cudaStream_t)stream;
+    auto fail = [&](const char* w) {
+        if (what) *what = w;
+        return CR_ERR_CUDA;
+    };
+    if (cudaMemsetAsync(f.scratch, 0, kCounterWords * 4, st) != cudaSuccess) return fail("counter reset");
+    const int64_t words = std::max<int64_t>(f.max_words, 1);
+    if (f.clear_before) {
+        const unsigned gx = (unsigned)std::min<int64_t>((words + 255) / 256, 4096);
+        k_mv_fill_views<<<dim3(gx, (unsigned)f.nviews), 256, 0, st>>>(
+            f.d_views, reinterpret_cast<unsigned long long*>(f.fbs), f.clear_value);
+        if (cudaGetLastError() != cudaSuccess) return fail("fill launch");
+    }
+    const int G = std::max(1, std::min(f.G, f.nviews));
+    const int ngroups = (f.nviews + G - 1) / G;
+    const int64_t nb = dispatched(f.ci, f.quirks);
+    const int64_t threads = nb * ngroups;
+    if (threads > 0) {
+        k_mv_cull<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+            f.d_views, f.d_files, f.nviews, f.ci.nfiles, G, ngroups, f.ci.batches, nb,
+            f.ci.capacity, f.quirks, f.culling, f.scratch);
+        if (cudaGetLastError() != cudaSuccess) return fail("cull launch");
+        MVArgs a;
+        a.views = f.d_views;
+        a.files = f.d_files;
+        a.nviews = f.nviews;
+        a.nfiles = f.ci.nfiles;
+        a.G = G;
+        a.batches = f.ci.batches;
+        a.lo = f.ci.lo;
+        a.md = f.ci.md;
+        a.hi = f.ci.hi;
+        a.rgba = f.ci.rgba;
+        a.fbs = reinterpret_cast<unsigned long long*>(f.fbs);
+        a.scratch = f.scratch;
+        a.list_cap = threads;  // k_mv_cull's list region: one item per (batch, group)
+        a.quirks = f.quirks;
+        const bool color = f.payload == CR_PAYLOAD_COLOR;
+        const int per_sm = f.ctas_per_sm > 0 ? f.ctas_per_sm
+                           : (color ? mv_occupancy_t<CR_PAYLOAD_COLOR>(f.block)
+                                    : mv_occupancy_t<CR_PAYLOAD_INDEX>(f.block));
+        const int grid = f.num_sms * per_sm;
+        const cudaError_t e = color ? launch_mv_raster_t<CR_PAYLOAD_COLOR>(a, f.block, grid, st)
+                                    : launch_mv_raster_t<CR_PAYLOAD_INDEX>(a, f.block, grid, st);
+        if (e != cudaSuccess) return fail("raster launch");
+    }
+    if (f.resolve) {
+        const unsigned gx = (unsigned)((words + 255) / 256);
+        k_mv_resolve<<<dim3(gx, (unsigned)f.nviews), 256, 0, st>>>(
+            f.d_views, reinterpret_cast<unsigned long long*>(f.fbs), f.images, f.ci.rgba,
+            f.ci.capacity, f.payload, f.clear_after, f.clear_value);
+        if (cudaGetLastError() != cudaSuccess) return fail("resolve launch");
+    }
+    return CR_OK;
+}
+
 }  // namespace cr
 
 using namespace cr;
@@ -380,7 +463,7 @@ struct cr_mv {
     int32_t nviews = 0;
     std::vector<int32_t> W, H;
     std::vector<int64_t> fb_off, img_off;
-    int64_t total_words = 0, total_pixels = 0, max_pixels = 0;
+    int64_t total_words = 0, total_pixels = 0, max_words = 0;
     unsigned long long* fbs = nullptr;
     uint32_t* images = nullptr;
     MVView* d_views = nullptr;
@@ -440,13 +523,6 @@ cr_status apply_params(cr_mv* mv, const cr_render_params* p) {
     return CR_OK;
 }
 
-int64_t dispatched_batches(const cr_mv* mv) {
-    int64_t nb = mv->ci.nb;
-    if (mv->quirks & CR_QUIRK_DISPATCH_BY_POINTS)
-        nb = std::min<int64_t>(nb, (mv->ci.n + kPointsPerBatch - 1) / kPointsPerBatch);
-    return nb;
-}
-
 cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
     const cr_render_params& p = mv->params;
     cudaError_t e = cudaMemcpyAsync(mv->d_views, mv->h_views, sizeof(MVView) * mv->nviews,
@@ -455,45 +531,30 @@ cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
         e = cudaMemcpyAsync(mv->d_files, mv->h_files,
                             sizeof(MVFile) * (size_t)mv->nviews * mv->ci.nfiles,
                             cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(mv->scratch, 0, kCounterWords * 4, st);
     if (e != cudaSuccess) return mv_cuda(mv, e, "frame setup");
-    const int64_t nb = dispatched_batches(mv);
-    const int64_t threads = nb * mv->ngroups;
-    if (threads > 0) {
-        k_mv_cull<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-            mv->d_views, mv->d_files, mv->nviews, mv->ci.nfiles, mv->G, mv->ngroups, mv->ci.batches,
-            nb, mv->ci.capacity, mv->quirks, p.frustum_culling, mv->scratch);
-        if ((e = cudaGetLastError()) != cudaSuccess) return mv_cuda(mv, e, "cull launch");
-        MVArgs a;
-        a.views = mv->d_views;
-        a.files = mv->d_files;
-        a.nviews = mv->nviews;
-        a.nfiles = mv->ci.nfiles;
-        a.G = mv->G;
-        a.batches = mv->ci.batches;
-        a.lo = mv->ci.lo;
-        a.md = mv->ci.md;
-        a.hi = mv->ci.hi;
-        a.rgba = mv->ci.rgba;
-        a.fbs = mv->fbs;
-        a.scratch = mv->scratch;
-        a.list_cap = threads;  // k_mv_cull's list region: one item per (batch, group)
-        a.quirks = mv->quirks;
-        int per_sm = p.ctas_per_sm > 0 ? p.ctas_per_sm
-                     : (p.payload == CR_PAYLOAD_COLOR ? mv_occupancy_t<CR_PAYLOAD_COLOR>(mv->block)
-                                                      : mv_occupancy_t<CR_PAYLOAD_INDEX>(mv->block));
-        const int grid = mv->num_sms * per_sm;
-        e = p.payload == CR_PAYLOAD_COLOR ? launch_mv_raster_t<CR_PAYLOAD_COLOR>(a, mv->block, grid, st)
-                                          : launch_mv_raster_t<CR_PAYLOAD_INDEX>(a, mv->block, grid, st);
-        if (e != cudaSuccess) return mv_cuda(mv, e, "raster launch");
-    }
-    if (p.resolve) {
-        const int64_t px = std::max<int64_t>(mv->max_pixels, 1);
-        dim3 grid((unsigned)((px + 255) / 256), (unsigned)mv->nviews);
-        k_mv_resolve<<<grid, 256, 0, st>>>(mv->d_views, mv->fbs, mv->images, mv->ci.rgba,
-                                           mv->ci.capacity, p.payload, p.clear_after, p.clear_value);
-        if ((e = cudaGetLastError()) != cudaSuccess) return mv_cuda(mv, e, "resolve launch");
-    }
+    MVFrame f{};
+    f.ci = mv->ci;
+    f.d_views = mv->d_views;
+    f.d_files = mv->d_files;
+    f.nviews = mv->nviews;
+    f.fbs = reinterpret_cast<uint64_t*>(mv->fbs);
+    f.images = mv->images;
+    f.scratch = mv->scratch;
+    f.G = mv->G;
+    f.block = mv->block;
+    f.ctas_per_sm = p.ctas_per_sm;
+    f.quirks = mv->quirks;
+    f.payload = p.payload;
+    f.culling = p.frustum_culling;
+    f.num_sms = mv->num_sms;
+    f.clear_before = 0;
+    f.resolve = p.resolve;
+    f.clear_after = p.clear_after;
+    f.clear_value = p.clear_value;
+    f.max_words = mv->max_words;
+    const char* what = "";
+    const cr_status s = mv_enqueue(f, st, &what);
+    if (s != CR_OK) return mv_cuda(mv, cudaGetLastError(), what);
     return CR_OK;
 }
 
@@ -529,7 +590,7 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
         mv->img_off.push_back(pixels);
         words += (int64_t)w * h + w + 1;
         pixels += (int64_t)w * h;
-        mv->max_pixels = std::max<int64_t>(mv->max_pixels, std::max<int64_t>((int64_t)w * h, w + 1));
+        mv->max_words = std::max<int64_t>(mv->max_words, (int64_t)w * h + w + 1);
     }
     if (words >= ((int64_t)1 << 32) - 1) {  // z-cache tags are 32-bit word offsets
         delete mv;
@@ -542,13 +603,12 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
         delete mv;
         return s;
     }
-    const int64_t items = mv->ci.nb * nviews;  // the work list at one view per group
     cudaError_t e = cudaMalloc(&mv->fbs, words * 8);
     if (e == cudaSuccess) e = cudaMalloc(&mv->images, std::max<int64_t>(pixels, 1) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&mv->d_views, sizeof(MVView) * nviews);
     if (e == cudaSuccess) e = cudaMalloc(&mv->d_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles);
-    if (e == cudaSuccess) e = cudaMalloc(&mv->scratch, (kScratchHead + 4 * items + 64) * 4);
-    if (e == cudaSuccess) e = cudaMemset(mv->scratch, 0, (kScratchHead + 4 * items + 64) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&mv->scratch, mv_scratch_words(mv->ci.nb, nviews) * 4);
+    if (e == cudaSuccess) e = cudaMemset(mv->scratch, 0, mv_scratch_words(mv->ci.nb, nviews) * 4);
     if (e == cudaSuccess) e = cudaHostAlloc(&mv->h_views, sizeof(MVView) * nviews, cudaHostAllocDefault);
     if (e == cudaSuccess)
         e = cudaHostAlloc(&mv->h_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles, cudaHostAllocDefault);
@@ -607,18 +667,9 @@ cr_status cr_mv_set_views(cr_mv* mv, const cr_view* views) {
     for (int v = 0; v < mv->nviews; v++) {
         if (views[v].width != mv->W[v] || views[v].height != mv->H[v])
             return mv_fail(mv, CR_ERR_INVALID_ARG, "view " + std::to_string(v) + " size differs from the plan");
-        ViewParams vp;
-        cr_status s = view_params_for(&views[v], mv->ci.box_min, mv->ci.nfiles, 1, &vp);
+        cr_status s = mv_fill_view(&views[v], mv->ci, &mv->h_views[v],
+                                   &mv->h_files[(int64_t)v * mv->ci.nfiles]);
         if (s != CR_OK) return mv_fail(mv, s, "view " + std::to_string(v) + ": bad matrices");
-        std::memcpy(mv->h_views[v].P, vp.P, sizeof(vp.P));
-        for (int f = 0; f < mv->ci.nfiles; f++) {
-            MVFile& o = mv->h_files[(int64_t)v * mv->ci.nfiles + f];
-            const FileRec& r = vp.files[f];
-            const int pick[12] = {0, 1, 3, 4, 5, 7, 8, 9, 11, 12, 13, 15};
-            for (int k = 0; k < 12; k++) o.T[k] = r.T[pick[k]];
-            std::memcpy(o.planes, r.planes, sizeof(o.planes));
-            std::memcpy(o.VW, r.VW, sizeof(o.VW));
-        }
     }
     mv->views_set = true;
     return CR_OK;

@@ -7,6 +7,9 @@ Seeded, so every run renders the same frames:
   * multiview_64       16 stereo pairs at 1440x1600 per eye (IPD 0.064 m,
                        parallel eye axes) flying over the cloud + 32 random
                        orbit poses at 512x512.
+  * serving            8 resident terrains of 10-500 M points, Poisson
+                       arrivals, clouds drawn Zipf(1.1), one random orbit
+                       camera per request at one of five resolutions.
 """
 from __future__ import annotations
 
@@ -79,3 +82,42 @@ def multiview_cloud_params(seed=4, extent=4500.0):
     """Terrain plus 2000 boxes (10-60 m tall, 20k points on their faces)."""
     return synth.synth_params(L.SYNTH_TERRAIN_BOXES, extent, seed, num_boxes=2000,
                               points_per_box=20000, box_min_height=10.0, box_max_height=60.0)
+
+
+SERVING_CLOUD_MPOINTS = (10, 25, 50, 100, 200, 300, 400, 500)
+SERVING_RESOLUTIONS = ((256, 256), (512, 512), (1280, 720), (1920, 1080), (3840, 2160))
+
+
+def serving_cloud_params(i: int, n: int):
+    """Terrain i of the serving set: the 1B-point terrain's density (10 points
+    per square metre), so the extent grows with sqrt(n)."""
+    return synth.synth_params(L.SYNTH_TERRAIN, math.sqrt(n / 10.0), 100 + i)
+
+
+def zipf_weights(k: int, s: float = 1.1) -> np.ndarray:
+    w = 1.0 / np.arange(1, k + 1, dtype=np.float64) ** s
+    return w / w.sum()
+
+
+def serving_requests(boxes, n: int, rate: float, seed: int = 5, zipf_s: float = 1.1,
+                     resolutions=SERVING_RESOLUTIONS):
+    """n requests with Poisson arrivals at `rate` per second.
+
+    boxes: [(box_min, box_max)] of the resident clouds, most popular first.
+    Returns (arrival_us[n], cameras) with cameras[i] = (cloud, view, proj, W, H).
+    """
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1e6 / rate, size=n)
+    arrival = np.cumsum(gaps) - gaps[0]
+    clouds = rng.choice(len(boxes), size=n, p=zipf_weights(len(boxes), zipf_s))
+    res = rng.integers(0, len(resolutions), size=n)
+    cams = []
+    for i in range(n):
+        c = int(clouds[i])
+        bmin, bmax = (np.asarray(b, float) for b in boxes[c])
+        _, _, radius, target = synth.zoom_to_cloud(bmin, bmax)
+        w, h = resolutions[int(res[i])]
+        view = synth.orbit_view(rng.uniform(-math.pi, math.pi), rng.uniform(-1.2, -0.3),
+                                radius * rng.uniform(0.5, 1.2), target)
+        cams.append((c, view, _perspective(60.0, w, h), w, h))
+    return arrival, cams

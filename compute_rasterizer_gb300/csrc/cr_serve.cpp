@@ -231,7 +231,10 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
     const int n = (int)sl.reqs.size();
     uint32_t* images = reinterpret_cast<uint32_t*>(s->pool);
     const int64_t nb = dispatched_batches(ci, s->quirks);
-    cudaError_t e = ensure_slot_scratch(sl, cr::mv_scratch_words(nb, c.plain_launches ? 1 : n));
+    // a launch of one request uses the single-view kernels: same image, and
+    // faster than the multi-view raster at one view per group
+    const bool single = c.plain_launches || n == 1;
+    cudaError_t e = ensure_slot_scratch(sl, cr::mv_scratch_words(nb, single ? 1 : n));
     if (e != cudaSuccess) {
         *what = "scratch allocation";
         return CR_ERR_OUT_OF_MEMORY;
@@ -242,7 +245,7 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
         *what = "scratch reset";
         return CR_ERR_CUDA;
     }
-    if (c.plain_launches) {
+    if (single) {
         // one reference frame per request: clear, cull, raster, resolve
         for (int i = 0; i < n; i++) {
             const Pending& p = sl.reqs[i];
@@ -273,7 +276,7 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
             bl.quirks = s->quirks;
             bl.payload = c.payload;
             bl.mode = cr::kModeRaster;
-            const int block = c.block_threads > 0 ? c.block_threads : 128;
+            const int block = c.plain_launches && c.block_threads > 0 ? c.block_threads : 128;
             const int per_sm = std::max(1, cr::batched_blocks_per_sm(bl.mode, bl.payload, block));
             if (cr::launch_batched(vp, bl, block, s->num_sms * per_sm, sl.st) != 0) {
                 *what = "plain raster launch";

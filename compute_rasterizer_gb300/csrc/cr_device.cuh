@@ -204,12 +204,17 @@ __device__ __forceinline__ bool zcache_rejects(const unsigned long long* zc, uin
     return (uint32_t)e == tag && wbits > (uint32_t)(e >> 32);
 }
 
-// Project a decoded point (render.cs:399-409 under the arithmetic contract).
-__device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, float z, int32_t& pix,
-                                        uint32_t& wbits) {
-    float px = __fmaf_rn(c.T8, z, __fmaf_rn(c.T4, y, __fmaf_rn(c.T0, x, c.T12)));
-    float py = __fmaf_rn(c.T9, z, __fmaf_rn(c.T5, y, __fmaf_rn(c.T1, x, c.T13)));
-    float pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
+// Clip-space position of a decoded point (render.cs:399-401).
+__device__ __forceinline__ void project_clip(const BatchCtx& c, float x, float y, float z,
+                                             float& px, float& py, float& pw) {
+    px = __fmaf_rn(c.T8, z, __fmaf_rn(c.T4, y, __fmaf_rn(c.T0, x, c.T12)));
+    py = __fmaf_rn(c.T9, z, __fmaf_rn(c.T5, y, __fmaf_rn(c.T1, x, c.T13)));
+    pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
+}
+
+// Divide, inside test and pixel (render.cs:402-409).
+__device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, float py, float pw,
+                                               int32_t& pix, uint32_t& wbits) {
     // render.cs:402 `pos.xyz / pos.w`: one correctly rounded reciprocal of w
     const float rw = __frcp_rn(pw);
     float qx = fmul(px, rw), qy = fmul(py, rw);
@@ -221,6 +226,14 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
     pix = ix + iy * c.W;
     wbits = __float_as_uint(pw);
     return in;
+}
+
+// Project a decoded point (render.cs:399-409 under the arithmetic contract).
+__device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, float z, int32_t& pix,
+                                        uint32_t& wbits) {
+    float px, py, pw;
+    project_clip(c, x, y, z, px, py, pw);
+    return project_finish(c, px, py, pw, pix, wbits);
 }
 
 }  // namespace

@@ -24,6 +24,7 @@
 //   k_resolve_* per-pixel resolves (resolve.cs files), optionally re-clearing.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "cr_internal.h"
@@ -228,55 +229,61 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
 // LIST 0: the 10-bit items (front of the list region), LIST 1: the 20/30-bit
 // items (back of the region).  Each list runs in its own instance, so the
 // common 10-bit instance carries no wider decode state (fewer registers).
+// List 1 is launched first and lets the list-0 grid start at once
+// (programmatic dependent launch); every list-0 CTA waits for the list-1 grid
+// before it exits, so work that follows on the stream sees both lists' writes.
 template <int MODE, int PAYLOAD, int BLOCK, int LIST>
 __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch bl) {
+    if (LIST == 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ uint32_t s_item[2];
     __shared__ unsigned long long s_zc[MODE == kModeHqsColor ? 1 : kZCacheSlots];
     uint32_t* cursor = bl.scratch + (LIST == 0 ? (MODE == kModeHqsColor ? kCursor1 : kCursor0)
                                                : (MODE == kModeHqsColor ? kCursor3 : kCursor2));
     const uint32_t nitems =
         *reinterpret_cast<volatile uint32_t*>(bl.scratch + (LIST == 0 ? kItemCount : kItemCount2));
-    if (nitems == 0) return;
-    if (MODE != kModeHqsColor)
-        for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
-    if (threadIdx.x == 0) s_item[0] = atomicAdd(cursor, 1u);
-    __syncthreads();
-    int buf = 0;
-    while (true) {
-        const uint32_t wi = s_item[buf];
-        if (wi >= nitems) break;
-        if (threadIdx.x == 0) s_item[buf ^ 1] = atomicAdd(cursor, 1u);
-        const uint32_t item =
-            bl.scratch[kScratchHead + (LIST == 0 ? (int64_t)wi : bl.list_cap - 1 - (int64_t)wi)];
-        const uint32_t b = item & 0x1FFFFFFFu;
-        const int level = (int)(item >> 29);
-
-        const int4* r4 = reinterpret_cast<const int4*>(bl.batches + b);
-        const int4 ra = __ldg(r4), rc = __ldg(r4 + 1), rd = __ldg(r4 + 2);
-        const float mnx = __int_as_float(ra.y), mny = __int_as_float(ra.z), mnz = __int_as_float(ra.w);
-        const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
-        const int64_t first = rd.x;
-        const int32_t count = (int32_t)points_in_batch(rc.w, bl.quirks);
-        const FileRec& f = vp.files[rd.y];
-
-        BatchCtx c;
-        const float steps = level >= 2 ? 1024.0f : 1073741824.0f;
-        c.mnx = mnx; c.mny = mny; c.mnz = mnz;
-        c.sx = __fdiv_rn(fsub(mxx, mnx), steps);
-        c.sy = __fdiv_rn(fsub(mxy, mny), steps);
-        c.sz = __fdiv_rn(fsub(mxz, mnz), steps);
-        c.T0 = f.T[0]; c.T1 = f.T[1]; c.T3 = f.T[3];
-        c.T4 = f.T[4]; c.T5 = f.T[5]; c.T7 = f.T[7];
-        c.T8 = f.T[8]; c.T9 = f.T[9]; c.T11 = f.T[11];
-        c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
-        c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
-        const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-        if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
-        else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, first, count, l0_x12);
-        else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, first, count, l0_x12);
+    if (nitems != 0) {
+        if (MODE != kModeHqsColor)
+            for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
+        if (threadIdx.x == 0) s_item[0] = atomicAdd(cursor, 1u);
         __syncthreads();
-        buf ^= 1;
+        int buf = 0;
+        while (true) {
+            const uint32_t wi = s_item[buf];
+            if (wi >= nitems) break;
+            if (threadIdx.x == 0) s_item[buf ^ 1] = atomicAdd(cursor, 1u);
+            const uint32_t item =
+                bl.scratch[kScratchHead + (LIST == 0 ? (int64_t)wi : bl.list_cap - 1 - (int64_t)wi)];
+            const uint32_t b = item & 0x1FFFFFFFu;
+            const int level = (int)(item >> 29);
+
+            const int4* r4 = reinterpret_cast<const int4*>(bl.batches + b);
+            const int4 ra = __ldg(r4), rc = __ldg(r4 + 1), rd = __ldg(r4 + 2);
+            const float mnx = __int_as_float(ra.y), mny = __int_as_float(ra.z), mnz = __int_as_float(ra.w);
+            const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
+            const int64_t first = rd.x;
+            const int32_t count = (int32_t)points_in_batch(rc.w, bl.quirks);
+            const FileRec& f = vp.files[rd.y];
+
+            BatchCtx c;
+            const float steps = level >= 2 ? 1024.0f : 1073741824.0f;
+            c.mnx = mnx; c.mny = mny; c.mnz = mnz;
+            c.sx = __fdiv_rn(fsub(mxx, mnx), steps);
+            c.sy = __fdiv_rn(fsub(mxy, mny), steps);
+            c.sz = __fdiv_rn(fsub(mxz, mnz), steps);
+            c.T0 = f.T[0]; c.T1 = f.T[1]; c.T3 = f.T[3];
+            c.T4 = f.T[4]; c.T5 = f.T[5]; c.T7 = f.T[7];
+            c.T8 = f.T[8]; c.T9 = f.T[9]; c.T11 = f.T[11];
+            c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
+            c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
+            const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
+            if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
+            else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, first, count, l0_x12);
+            else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, first, count, l0_x12);
+            __syncthreads();
+            buf ^= 1;
+        }
     }
+    if (LIST == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // ---- plain 16 B/point path --------------------------------------------------
@@ -440,22 +447,49 @@ int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb, int64
     return launch_status();
 }
 
-template <int MODE, int PAYLOAD, int LIST>
-static void launch_list(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
-                        cudaStream_t s) {
-    switch (block) {
-        case 128: k_batched<MODE, PAYLOAD, 128, LIST><<<grid, 128, 0, s>>>(vp, bl); break;
-        case 512: k_batched<MODE, PAYLOAD, 512, LIST><<<grid, 512, 0, s>>>(vp, bl); break;
-        default: k_batched<MODE, PAYLOAD, 256, LIST><<<grid, 256, 0, s>>>(vp, bl); break;
-    }
+template <int MODE, int PAYLOAD, int BLOCK>
+static int occupancy_list1() {
+    static const int n = [] {
+        int k = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_batched<MODE, PAYLOAD, BLOCK, 1>,
+                                                             BLOCK, 0) == cudaSuccess && k > 0
+                   ? k
+                   : 1;
+    }();
+    return n;
 }
 
-// The 10-bit list, then the (usually short) 20/30-bit list.
+// The (usually short) 20/30-bit list with a grid that is resident at once,
+// then the 10-bit list as its programmatic dependent: it starts as soon as
+// every list-1 CTA has started, on the SM room list 1 leaves.
+template <int MODE, int PAYLOAD, int BLOCK>
+static void launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid, cudaStream_t s) {
+    int device = 0, sms = 1;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int grid1 = std::min(grid, sms * occupancy_list1<MODE, PAYLOAD, BLOCK>());
+    k_batched<MODE, PAYLOAD, BLOCK, 1><<<grid1, BLOCK, 0, s>>>(vp, bl);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0>, vp, bl);
+}
+
 template <int MODE, int PAYLOAD>
 static void launch_batched_t(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
                              cudaStream_t s) {
-    launch_list<MODE, PAYLOAD, 0>(vp, bl, block, grid, s);
-    launch_list<MODE, PAYLOAD, 1>(vp, bl, block, grid, s);
+    switch (block) {
+        case 128: launch_lists<MODE, PAYLOAD, 128>(vp, bl, grid, s); break;
+        case 512: launch_lists<MODE, PAYLOAD, 512>(vp, bl, grid, s); break;
+        default: launch_lists<MODE, PAYLOAD, 256>(vp, bl, grid, s); break;
+    }
 }
 
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid, void* stream) {

@@ -188,7 +188,7 @@ __device__ __forceinline__ void splat_view(const MVArgs& a, unsigned long long* 
 // LIST 0: items whose visible views all decode at 10 bit (only the low word
 // stream is read); LIST 1: the others, each view decoded at its own level.
 template <int PAYLOAD, int BLOCK, int LIST>
-__global__ void __launch_bounds__(BLOCK) k_mv_raster(MVArgs a) {
+__device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
     __shared__ uint32_t s_item[2];
     __shared__ __align__(16) float s_view[CR_MV_MAX_GROUP][kSlotWords];
     __shared__ unsigned long long s_zc[kZCacheSlots];
@@ -291,6 +291,15 @@ __global__ void __launch_bounds__(BLOCK) k_mv_raster(MVArgs a) {
     }
 }
 
+// List 1 is launched first and lets the list-0 grid start at once
+// (programmatic dependent launch); every list-0 CTA waits for the list-1 grid
+// before it exits, so the resolve that follows sees both lists' writes.
+template <int PAYLOAD, int BLOCK, int LIST>
+__global__ void __launch_bounds__(BLOCK) k_mv_raster(MVArgs a) {
+    if (LIST == 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    mv_raster_items<PAYLOAD, BLOCK, LIST>(a);
+    if (LIST == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 
 __global__ void k_mv_resolve(const MVView* __restrict__ views, unsigned long long* fbs,
                              uint32_t* images, const uint32_t* __restrict__ rgba,
@@ -336,22 +345,49 @@ __global__ void k_mv_fill_views(const MVView* __restrict__ views, unsigned long 
 }
 
 // The 10-bit list, then the 20/30-bit list, on one stream.
-template <int PAYLOAD, int LIST>
-void launch_mv_list(const MVArgs& a, int block, int grid, cudaStream_t s) {
-    switch (block) {
-        case 64: k_mv_raster<PAYLOAD, 64, LIST><<<grid, 64, 0, s>>>(a); break;
-        case 256: k_mv_raster<PAYLOAD, 256, LIST><<<grid, 256, 0, s>>>(a); break;
-        default: k_mv_raster<PAYLOAD, 128, LIST><<<grid, 128, 0, s>>>(a); break;
-    }
+template <int PAYLOAD, int BLOCK>
+int mv_occupancy_list1() {
+    static const int n = [] {
+        int k = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_mv_raster<PAYLOAD, BLOCK, 1>, BLOCK,
+                                                             0) == cudaSuccess && k > 0
+                   ? k
+                   : 1;
+    }();
+    return n;
+}
+
+// The 20/30-bit list with a grid that is resident at once, then the 10-bit
+// list as its programmatic dependent.
+template <int PAYLOAD, int BLOCK>
+cudaError_t launch_mv_lists(const MVArgs& a, int grid, cudaStream_t s) {
+    int device = 0, sms = 1;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int grid1 = std::min(grid, sms * mv_occupancy_list1<PAYLOAD, BLOCK>());
+    k_mv_raster<PAYLOAD, BLOCK, 1><<<grid1, BLOCK, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(BLOCK);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_mv_raster<PAYLOAD, BLOCK, 0>, a);
 }
 
 template <int PAYLOAD>
 cudaError_t launch_mv_raster_t(const MVArgs& a, int block, int grid, cudaStream_t s) {
-    launch_mv_list<PAYLOAD, 0>(a, block, grid, s);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    launch_mv_list<PAYLOAD, 1>(a, block, grid, s);
-    return cudaGetLastError();
+    switch (block) {
+        case 64: return launch_mv_lists<PAYLOAD, 64>(a, grid, s);
+        case 256: return launch_mv_lists<PAYLOAD, 256>(a, grid, s);
+        default: return launch_mv_lists<PAYLOAD, 128>(a, grid, s);
+    }
 }
 
 template <int PAYLOAD>

@@ -1,4 +1,4 @@
-"""ctypes binding of include/cr_raster.h, include/cr_synth.h and include/cr_serve.h.
+"""ctypes binding of include/cr_raster.h, cr_synth.h, cr_serve.h and cr_las.h.
 
 The CUDA library is built in-tree (compute_rasterizer_gb300/_build/libcr_raster.so
 by compute_rasterizer_gb300.build).  There is no CPU fallback: loading fails
@@ -108,6 +108,17 @@ class ServerStats(C.Structure):
                 ("queued", C.c_int32), ("gpu_ms", C.c_double)]
 
 
+class LasInfo(C.Structure):
+    _fields_ = [("num_points", C.c_int64), ("offset_to_points", C.c_int64),
+                ("version_major", C.c_int32), ("version_minor", C.c_int32),
+                ("point_format", C.c_int32), ("bytes_per_point", C.c_int32),
+                ("scale", C.c_double * 3), ("offset", C.c_double * 3),
+                ("min", C.c_double * 3), ("max", C.c_double * 3)]
+
+
+LAS_MIN_HEADER, LAS_14_HEADER = 227, 375
+MAX_POINTS_PER_LOAD = 1024000
+
 SERVE_MAX_POOL_BYTES = 16 << 30
 SERVE_MAX_BATCH_VIEWS = 256
 
@@ -179,6 +190,10 @@ _SIGS = {
     "cr_synth_cloud_device": (I32, [P, C.POINTER(SynthParams), I64, P, C.POINTER(LasHeader), P]),
     "cr_synth_uniform_host": (I32, [U64, I64, FLT, P]),
     "cr_synth_uniform_device": (I32, [P, U64, I64, FLT, P, P]),
+    # cr_las.h
+    "cr_las_parse_header": (I32, [P, I64, C.POINTER(LasInfo)]),
+    "cr_cloud_load_las": (I32, [P, P, P, I64, C.POINTER(LasInfo), I64, I64, I32, P]),
+    "cr_las_num_batches": (I64, [I64]),
     # cr_serve.h
     "cr_server_create": (I32, [P, C.POINTER(ServerConfig), PP]),
     "cr_server_destroy": (I32, [P]),

@@ -101,3 +101,19 @@ def handmade_cloud(points, colors, box_min=(-1.0, -1.0, 0.0), box_max=(1.0, 1.0,
 
 def identity_cam(w=64, h=32):
     return (IDENTITY, IDENTITY, w, h)
+
+
+def build_method_demo(out_dir):
+    """Compiles tests/cpp/method_demo.cpp against include/cr_method.hpp and the
+    in-tree library; returns the executable's path."""
+    import subprocess
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    libdir = root / "compute_rasterizer_gb300" / "_build"
+    exe = Path(out_dir) / "method_demo"
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}",
+           str(root / "tests" / "cpp" / "method_demo.cpp"), f"-L{libdir}", "-lcr_raster",
+           f"-Wl,-rpath,{libdir}", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    return exe

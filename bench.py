@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--serving", default="quick", choices=["quick", "full", "off"])
+    ap.add_argument("--extras", default="payloads,multiview,configs,serving",
+                    help="comma list of extra workloads after the headline frame")
     return ap.parse_args()
 
 
@@ -312,16 +314,20 @@ def main():
            "gpu_launches": 3 * args.steps, "clocks": clk}
 
     if not args.no_extras:
-        out["extras"] = extras(ctx, cloud, cv, fb, sh, n, args)
-        try:
-            out["extras"]["multiview_64"] = multiview_64(ctx, sh, args.steps, payload)
-        except Exception as exc:  # the headline line is printed regardless
-            out["extras"]["multiview_64"] = {"error": repr(exc)}
+        out["extras"] = {}
+        want = set(args.extras.split(","))
+        runs = [("payloads", lambda: extras(ctx, cloud, cv, fb, sh, n, args)),
+                ("multiview", lambda: {"multiview_64": multiview_64(ctx, sh, args.steps, payload)}),
+                ("configs", lambda: small_configs(ctx, sh, args, payload))]
         if args.serving != "off":
+            runs.append(("serving", lambda: {"serving": serving(ctx, sh, args, payload)}))
+        for name, fn in runs:
+            if name not in want:
+                continue
             try:
-                out["extras"]["serving"] = serving(ctx, sh, args, payload)
-            except Exception as exc:
-                out["extras"]["serving"] = {"error": repr(exc)}
+                out["extras"].update(fn())
+            except Exception as exc:  # the headline line is printed regardless
+                out["extras"][name] = {"error": repr(exc)}
     if not args.no_e2e:
         out["e2e"] = e2e(ctx, cloud, cv, params, fb, sh, n, args, bmin)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -415,6 +421,83 @@ def multiview_64(ctx, sh, steps, payload):
     mv.close()
     for f in fbs:
         f.close()
+    cloud.close()
+    return out
+
+
+def small_configs(ctx, sh, args, payload):
+    """The plain 16 B path at 4,194,304 points and 1920x1080 (early-z, the
+    reference's uniform-cube scene), and the 100M-point terrain seen from 5
+    flight-path poses at 2560x1440 (batched adaptive path, culling on).
+    Roofline: algorithmic bytes per frame / frame time, against the measured
+    copy bandwidth."""
+    import torch
+
+    import compute_rasterizer_gb300 as cr
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import synth, workloads
+    stream = torch.cuda.ExternalStream(sh)
+    peak, _ = measured_peaks()
+    k = max(10, min(args.steps, 100))
+
+    def timed(fn, frames):
+        for _ in range(3):
+            fn()
+        ctx.sync(sh)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
+            fn()
+        e1.record(stream)
+        ctx.sync(sh)
+        return e0.elapsed_time(e1) / frames
+
+    out = {}
+    n1, W1, H1 = 4_194_304, 1920, 1080
+    cloud = synth.uniform_cloud_device(ctx, 1, n1, 100.0, sh)
+    view = synth.look_at([150.0, 150.0, 150.0], [50.0, 50.0, 50.0], [0.0, 0.0, 1.0])
+    cv = cr.make_view(view, synth.perspective(60.0, W1 / H1, 0.1, 1000.0), W1, H1)
+    fb = ctx.framebuffer(W1, H1)
+    fb.clear(0xFFFFFFFFFFFFFFFF, stream=sh)
+    p = cr.default_params(L.METHOD_EARLYZ)  # resolve + re-clear, as the reference's frame
+    ms = timed(lambda: ctx.render(cloud, cv, p, fb, sh), k)
+    P = W1 * H1
+    bytes1 = 16 * n1 + 8 * P + 4 * P + 8 * P
+    out["plain_4m_1080p"] = {
+        "points": n1, "ms_per_frame": round(ms, 4), "gpoints_per_s": round(n1 / ms / 1e6, 2),
+        "algorithmic_bytes": bytes1, "achieved_gbs": round(bytes1 / ms / 1e6, 1),
+        "frac_of_measured_hbm": round(bytes1 / ms / 1e6 / peak, 4),
+        "frame": "early-z raster (16 B/point) + resolve + re-clear"}
+    fb.close()
+    cloud.close()
+
+    n2 = 100_000_000
+    cloud, hdr = synth.build_cloud_device(ctx, synth.synth_params(L.SYNTH_TERRAIN, 1000.0, 2), n2, sh)
+    cams = workloads.flight_path(np.array(hdr.min[:]), np.array(hdr.max[:]))
+    p = cr.default_params(L.METHOD_LOOP_LAS, payload=payload)
+    poses = []
+    for view, proj, W, H in cams:
+        cv = cr.make_view(view, proj, W, H)
+        fb = ctx.framebuffer(W, H)
+        fb.clear(stream=sh)
+        ms = timed(lambda: ctx.render(cloud, cv, p, fb, sh), k)
+        st = ctx.frame_stats(cloud, p)
+        P = W * H
+        gather = 4 * P if payload == L.PAYLOAD_INDEX else 0
+        fbytes = int(st.stream_bytes) + 20 * P + gather
+        poses.append({"ms_per_frame": round(ms, 4), "gpoints_per_s": round(n2 / ms / 1e6, 2),
+                      "batches_visible": int(st.batches_visible),
+                      "points_per_level": list(st.points_per_level),
+                      "algorithmic_bytes": fbytes,
+                      "frac_of_measured_hbm": round(fbytes / ms / 1e6 / peak, 4)})
+        fb.close()
+    total = sum(q["ms_per_frame"] for q in poses)
+    out["flight_100m_1440p"] = {
+        "points": n2, "poses": poses, "mean_ms_per_frame": round(total / len(poses), 4),
+        "gpoints_per_s": round(n2 * len(poses) / total / 1e6, 2),
+        "payload": "color" if payload == L.PAYLOAD_COLOR else "index",
+        "frame": "cull + raster + resolve + re-clear; bytes = coordinate/color words of visible "
+                 "batches at their levels + 64 B per visible batch + 20 B per pixel"}
     cloud.close()
     return out
 

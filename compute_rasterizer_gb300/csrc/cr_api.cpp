@@ -168,7 +168,8 @@ cr_status build_view_params(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* v
 }
 
 cr_status check_size(cr_ctx* ctx, int32_t W, int32_t H) {
-    // pixel ids stay below 2^31 and truncation via the 2^23 trick needs W, H < 2^22
+    // pixel ids stay below 2^31; W, H < 2^22 keeps (q * 0.5 + 0.5) * W below
+    // 2^22, where a float still resolves fractions of a pixel
     if (W <= 0 || H <= 0 || W >= (1 << 22) || H >= (1 << 22) ||
         (int64_t)W * H + W + 1 >= ((int64_t)1 << 31))
         return fail(ctx, CR_ERR_INVALID_ARG, "bad framebuffer size %s%lld", "", (long long)W * H);

@@ -339,11 +339,14 @@ def main():
 
 
 def extras(ctx, cloud, cv, fb, sh, n, args):
-    """The same frame with the index payload (loop_las as registered) and HQS."""
+    """The same frame with the index payload (loop_las as registered) and HQS,
+    timed with CUDA events; HQS also per pass, with its roofline fraction."""
     import torch
 
     import compute_rasterizer_gb300 as cr
     from compute_rasterizer_gb300 import _lib as L
+    stream = torch.cuda.ExternalStream(sh)
+    peak, _ = measured_peaks()
     res = {}
     k = max(5, min(args.steps, 50))
     for name, method, payload, kind in (("index_payload", L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX, L.FB_U64),
@@ -353,76 +356,31 @@ def extras(ctx, cloud, cv, fb, sh, n, args):
         p = cr.default_params(method, payload=payload)
         for _ in range(3):
             ctx.render(cloud, cv, p, f, sh)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        ctx.sync(sh)
+        ctx.timing_enable(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         for _ in range(k):
             ctx.render(cloud, cv, p, f, sh)
+        e1.record(stream)
         ctx.sync(sh)
-        dt = (time.perf_counter() - t0) / k
-        res[name] = {"ms_per_frame": round(dt * 1e3, 4), "gpoints_per_s": round(n / dt / 1e9, 3)}
+        ms = e0.elapsed_time(e1) / k
+        r = {"ms_per_frame": round(ms, 4), "gpoints_per_s": round(n / ms / 1e6, 3)}
+        stages = {"cull": L.STAGE_CULL, "raster": L.STAGE_RASTER, "resolve": L.STAGE_RESOLVE}
+        if kind == L.FB_HQS:
+            stages = {"cull": L.STAGE_CULL, "depth_pass": L.STAGE_RASTER,
+                      "color_pass": L.STAGE_HQS_COLOR, "resolve": L.STAGE_RESOLVE}
+        r["stages_ms"] = {s: round(float(np.mean(ctx.timing_read(v, k))), 4) for s, v in stages.items()}
+        ctx.timing_enable(0)
+        st = ctx.frame_stats(cloud, p)
+        P = fb.W * fb.H
+        # stream words of both passes + depth/accumulator clear, resolve read, image write
+        fbytes = int(st.stream_bytes) + (20 * P + 20 * P + 4 * P if kind == L.FB_HQS else 20 * P + 4 * P)
+        r["algorithmic_bytes"] = fbytes
+        r["frac_of_measured_hbm"] = round(fbytes / ms / 1e6 / peak, 4)
+        res[name] = r
         f.close()
     return res
-
-
-def multiview_64(ctx, sh, steps, payload):
-    """200M points (terrain + 2000 boxes), 64 views: the multi-view plan
-    (autotuned, CUDA graph) against one cr_render per view, images compared."""
-    import torch
-
-    import compute_rasterizer_gb300 as cr
-    from compute_rasterizer_gb300 import _lib as L
-    from compute_rasterizer_gb300 import synth, workloads
-    from compute_rasterizer_gb300.multiview import MultiView
-    n = 200_000_000
-    cloud, hdr = synth.build_cloud_device(ctx, workloads.multiview_cloud_params(), n, sh)
-    cams = workloads.multiview_64(np.array(hdr.min[:]), np.array(hdr.max[:]))
-    views = [cr.make_view(*c) for c in cams]
-    params = cr.default_params(L.METHOD_LOOP_LAS, payload=payload)
-    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
-    mv.set_views(views)
-    mv.clear(stream=sh)
-    best, report = mv.autotune(frames=3, stream=sh)
-    k = max(3, min(steps, 20))
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    stream = torch.cuda.ExternalStream(sh)
-    for _ in range(3):
-        mv.render(True, sh)
-    ctx.sync(sh)
-    ev[0].record(stream)
-    for _ in range(k):
-        mv.render(True, sh)
-    ev[1].record(stream)
-    ctx.sync(sh)
-    mv_ms = ev[0].elapsed_time(ev[1]) / k
-    fbs = [ctx.framebuffer(c[2], c[3]) for c in cams]
-    for f in fbs:
-        f.clear(stream=sh)
-    for v, f in zip(views, fbs):
-        ctx.render(cloud, v, params, f, sh)
-    ctx.sync(sh)
-    ev[2].record(stream)
-    for _ in range(k):
-        for v, f in zip(views, fbs):
-            ctx.render(cloud, v, params, f, sh)
-    ev[3].record(stream)
-    ctx.sync(sh)
-    plain_ms = ev[2].elapsed_time(ev[3]) / k
-    same = all(np.array_equal(mv.read(i, L.FB_IMAGE, sh), f.read(L.FB_IMAGE, sh))
-               for i, f in enumerate(fbs))
-    out = {"points": n, "views": len(cams), "payload": "color" if payload else "index",
-           "batched_ms_per_frame": round(mv_ms, 3), "plain_ms_per_frame": round(plain_ms, 3),
-           "batched_frames_per_s": round(1e3 / mv_ms, 2), "plain_frames_per_s": round(1e3 / plain_ms, 2),
-           "speedup_vs_plain": round(plain_ms / mv_ms, 3), "bit_exact_images": bool(same),
-           "autotuned": {"block_threads": best.block_threads, "views_per_group": best.views_per_group,
-                         "points_per_thread": 10240 // max(1, best.block_threads)},
-           "autotune_ms": report,
-           "plain": "64 x cr_render (cull + raster + resolve per view), same stream",
-           "batched": "one multi-view plan frame (one cull, one persistent raster, one resolve), CUDA graph"}
-    mv.close()
-    for f in fbs:
-        f.close()
-    cloud.close()
-    return out
 
 
 def small_configs(ctx, sh, args, payload):

@@ -122,38 +122,26 @@ struct Emit<kModeHqsDepth> {
     }
 };
 
-template <>
-struct Emit<kModeHqsColor> {
-    static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long*,
-                                               bool ok, int32_t pix, uint32_t wbits, uint32_t,
-                                               uint32_t color) {
-        bool vis = false;
-        if (ok) {
-            // the depth buffer is read-only during this pass
-            const uint32_t d = __ldg(bl.depth + pix);
-            // color.cs:399-403: depth <= bufferDepth * 1.01
-            vis = __uint_as_float(wbits) <= fmul(__uint_as_float(d), 1.01f);
-        }
-        if (__any_sync(kFull, vis)) {
-            // color.cs:408-441: partitioned sums of (R, G, B, 1), leader adds
-            const uint32_t peers = __match_any_sync(kFull, vis ? (uint32_t)pix : kNoPixel);
-            if (vis) {
-                const uint32_t rg = (color & 0xFFu) | (((color >> 8) & 0xFFu) << 16);
-                const uint32_t bc = ((color >> 16) & 0xFFu) | (1u << 16);
-                const uint32_t srg = __reduce_add_sync(peers, rg);
-                const uint32_t sbc = __reduce_add_sync(peers, bc);
-                if (lane_id() == (uint32_t)(__ffs(peers) - 1)) {
-                    unsigned long long* a =
-                        reinterpret_cast<unsigned long long*>(bl.accum) + 2 * (int64_t)pix;
-                    atomicAdd(a, (unsigned long long)(srg & 0xFFFFu) |
-                                     ((unsigned long long)(srg >> 16) << 32));
-                    atomicAdd(a + 1, (unsigned long long)(sbc & 0xFFFFu) |
-                                         ((unsigned long long)(sbc >> 16) << 32));
-                }
-            }
+// HQS color pass (color.cs:399-441): the sums of (R, G, B, 1) over the points
+// of a lane's run (consecutive in-view points on one pixel, see run_points)
+// join the warp's partitioned sum over lanes on the same pixel; the leader adds
+// them to the pixel's two 64-bit accumulators.  All sums are integer adds, so
+// the accumulators equal one add per point in any order.  Per lane a run has
+// at most 4 points, so the 16-bit fields hold a warp's sums (32 x 4 x 255).
+__device__ __forceinline__ void hqs_color_flush(const BatchedLaunch& bl, bool active, uint32_t pix,
+                                                uint32_t rg, uint32_t bc) {
+    if (!__any_sync(kFull, active)) return;
+    const uint32_t peers = __match_any_sync(kFull, active ? pix : kNoPixel);
+    if (active) {
+        const uint32_t srg = __reduce_add_sync(peers, rg);
+        const uint32_t sbc = __reduce_add_sync(peers, bc);
+        if (lane_id() == (uint32_t)(__ffs(peers) - 1)) {
+            unsigned long long* a = reinterpret_cast<unsigned long long*>(bl.accum) + 2 * (int64_t)pix;
+            atomicAdd(a, (unsigned long long)(srg & 0xFFFFu) | ((unsigned long long)(srg >> 16) << 32));
+            atomicAdd(a + 1, (unsigned long long)(sbc & 0xFFFFu) | ((unsigned long long)(sbc >> 16) << 32));
         }
     }
-};
+}
 
 // LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0).
 // Points [first, first + count) are read as 128-bit vectors starting at the
@@ -191,6 +179,12 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             if (kNeedColor) ncol = ld_stream(co4 + vn);
         }
         const int32_t rel0 = 4 * v - head;  // batch-local index of word 0
+        // HQS color: the lane's run of consecutive in-view points on one pixel
+        // (Morton order puts most of a lane's 4 points on the same pixel): one
+        // depth read per run, colors summed in registers, one flush per run
+        uint32_t run_pix = kNoPixel, run_rg = 0, run_bc = 0;
+        float run_lim = 0.0f;
+        bool run_open = false;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const bool valid = (uint32_t)(rel0 + j) < (uint32_t)count;
@@ -220,9 +214,28 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             uint32_t wbits;
             const bool ok = project(c, x, y, z, pix, wbits) && valid;
             const uint32_t color = kNeedColor ? u4get(col, j) : 0u;
-            const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? color : (uint32_t)idx;
-            Emit<MODE>::run(bl, zc, ok, pix, wbits, payload, color);
+            if constexpr (MODE == kModeHqsColor) {
+                const bool cont = run_open && ok && (uint32_t)pix == run_pix;
+                hqs_color_flush(bl, run_open && !cont && run_bc != 0u, run_pix, run_rg, run_bc);
+                if (ok && !cont) {
+                    // the depth buffer is read-only during this pass
+                    run_pix = (uint32_t)pix;
+                    run_rg = run_bc = 0u;
+                    run_lim = fmul(__uint_as_float(__ldg(bl.depth + pix)), 1.01f);
+                }
+                // color.cs:399-403: depth <= bufferDepth * 1.01
+                if (ok && __uint_as_float(wbits) <= run_lim) {
+                    run_rg += (color & 0xFFu) | (((color >> 8) & 0xFFu) << 16);
+                    run_bc += ((color >> 16) & 0xFFu) | (1u << 16);
+                }
+                run_open = ok;
+            } else {
+                const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? color : (uint32_t)idx;
+                Emit<MODE>::run(bl, zc, ok, pix, wbits, payload, color);
+            }
         }
+        if constexpr (MODE == kModeHqsColor)
+            hqs_color_flush(bl, run_open && run_bc != 0u, run_pix, run_rg, run_bc);
     }
 }
 

@@ -311,7 +311,8 @@ def main():
            "frame_stats": {"batches_visible": int(stats.batches_visible),
                            "batches_dispatched": int(stats.batches_dispatched),
                            "points_per_level": list(stats.points_per_level)},
-           "gpu_launches": 3 * args.steps, "clocks": clk}
+           "gpu_launches": 4 * args.steps,  # cull, raster list 1, raster list 0, resolve
+           "clocks": clk}
 
     if not args.no_extras:
         out["extras"] = {}

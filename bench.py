@@ -384,6 +384,67 @@ def extras(ctx, cloud, cv, fb, sh, n, args):
     return res
 
 
+def multiview_64(ctx, sh, steps, payload):
+    """200M points (terrain + 2000 boxes), 64 views: the multi-view plan
+    (autotuned, CUDA graph) against one cr_render per view, images compared."""
+    import torch
+
+    import compute_rasterizer_gb300 as cr
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import synth, workloads
+    from compute_rasterizer_gb300.multiview import MultiView
+    n = 200_000_000
+    cloud, hdr = synth.build_cloud_device(ctx, workloads.multiview_cloud_params(), n, sh)
+    cams = workloads.multiview_64(np.array(hdr.min[:]), np.array(hdr.max[:]))
+    views = [cr.make_view(*c) for c in cams]
+    params = cr.default_params(L.METHOD_LOOP_LAS, payload=payload)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views(views)
+    mv.clear(stream=sh)
+    best, report = mv.autotune(frames=3, stream=sh)
+    k = max(3, min(steps, 20))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stream = torch.cuda.ExternalStream(sh)
+    for _ in range(3):
+        mv.render(True, sh)
+    ctx.sync(sh)
+    ev[0].record(stream)
+    for _ in range(k):
+        mv.render(True, sh)
+    ev[1].record(stream)
+    ctx.sync(sh)
+    mv_ms = ev[0].elapsed_time(ev[1]) / k
+    fbs = [ctx.framebuffer(c[2], c[3]) for c in cams]
+    for f in fbs:
+        f.clear(stream=sh)
+    for v, f in zip(views, fbs):
+        ctx.render(cloud, v, params, f, sh)
+    ctx.sync(sh)
+    ev[2].record(stream)
+    for _ in range(k):
+        for v, f in zip(views, fbs):
+            ctx.render(cloud, v, params, f, sh)
+    ev[3].record(stream)
+    ctx.sync(sh)
+    plain_ms = ev[2].elapsed_time(ev[3]) / k
+    same = all(np.array_equal(mv.read(i, L.FB_IMAGE, sh), f.read(L.FB_IMAGE, sh))
+               for i, f in enumerate(fbs))
+    out = {"points": n, "views": len(cams), "payload": "color" if payload else "index",
+           "batched_ms_per_frame": round(mv_ms, 3), "plain_ms_per_frame": round(plain_ms, 3),
+           "batched_frames_per_s": round(1e3 / mv_ms, 2), "plain_frames_per_s": round(1e3 / plain_ms, 2),
+           "speedup_vs_plain": round(plain_ms / mv_ms, 3), "bit_exact_images": bool(same),
+           "autotuned": {"block_threads": best.block_threads, "views_per_group": best.views_per_group,
+                         "points_per_thread": 10240 // max(1, best.block_threads)},
+           "autotune_ms": report,
+           "plain": "64 x cr_render (cull + raster + resolve per view), same stream",
+           "batched": "one multi-view plan frame (one cull, one persistent raster, one resolve), CUDA graph"}
+    mv.close()
+    for f in fbs:
+        f.close()
+    cloud.close()
+    return out
+
+
 def small_configs(ctx, sh, args, payload):
     """The plain 16 B path at 4,194,304 points and 1920x1080 (early-z, the
     reference's uniform-cube scene), and the 100M-point terrain seen from 5
@@ -427,6 +488,14 @@ def small_configs(ctx, sh, args, payload):
         "algorithmic_bytes": bytes1, "achieved_gbs": round(bytes1 / ms / 1e6, 1),
         "frac_of_measured_hbm": round(bytes1 / ms / 1e6 / peak, 4),
         "frame": "early-z raster (16 B/point) + resolve + re-clear"}
+    # the reference's warp-reduction variants of the same frame (2021 dedup,
+    # early-z & reduce): same bytes, different per-point atomics
+    for key, m in (("plain_4m_1080p_dedup", L.METHOD_DEDUP),
+                   ("plain_4m_1080p_earlyz_reduce", L.METHOD_EARLYZ_REDUCE)):
+        pm = cr.default_params(m)
+        ms = timed(lambda: ctx.render(cloud, cv, pm, fb, sh), k)
+        out[key] = {"ms_per_frame": round(ms, 4), "gpoints_per_s": round(n1 / ms / 1e6, 2),
+                    "frac_of_measured_hbm": round(bytes1 / ms / 1e6 / peak, 4)}
     fb.close()
     cloud.close()
 

@@ -20,7 +20,8 @@ OK, INVALID_ARG, OUT_OF_MEMORY, ADMISSION_REJECTED, TIMEOUT, CUDA_ERROR, DEVICE_
     UNSUPPORTED, NOT_FOUND = range(9)
 
 # methods / payloads / quirks / streams / fb kinds
-METHOD_LOOP_LAS, METHOD_LOOP_LAS_PREFETCH, METHOD_LOOP_LAS_HQS, METHOD_EARLYZ = range(4)
+METHOD_LOOP_LAS, METHOD_LOOP_LAS_PREFETCH, METHOD_LOOP_LAS_HQS, METHOD_EARLYZ, METHOD_DEDUP, \
+    METHOD_EARLYZ_REDUCE = range(6)
 PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
 QUIRK_L0_X12, QUIRK_INCLUSIVE_END, QUIRK_DISPATCH_BY_POINTS = 1, 2, 4
 QUIRKS_METHOD_DEFAULT = -1
@@ -53,7 +54,8 @@ class RenderParams(C.Structure):
                 ("frustum_culling", C.c_int32), ("resolve", C.c_int32),
                 ("clear_after", C.c_int32), ("clear_value", C.c_uint64),
                 ("block_threads", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("views_per_group", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("views_per_group", C.c_int32), ("lod_skip_level", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class LasHeader(C.Structure):

@@ -192,16 +192,28 @@ cr_status ensure_scratch(cr_ctx* ctx, int64_t items) {
     return CR_OK;
 }
 
-const char* kNames[4] = {"loop_las", "loop_las_prefetch", "loop_las_hqs", "(2021) early-z"};
-const char* kGroups[4] = {"10-10-10 bit encoded", "10-10-10 bit encoded", "10-10-10 bit encoded",
-                          "2021 method; standard 16 byte per point"};
-const char* kDescriptions[4] = {
+constexpr int kNumMethods = 6;
+const char* kNames[kNumMethods] = {"loop_las",       "loop_las_prefetch", "loop_las_hqs",
+                                   "(2021) early-z", "(2021) dedup",      "(2021) early-z & reduce"};
+const char* kGroups[kNumMethods] = {"10-10-10 bit encoded", "10-10-10 bit encoded", "10-10-10 bit encoded",
+                                    "2021 method; standard 16 byte per point",
+                                    "2021 method; standard 16 byte per point",
+                                    "2021 method; standard 16 byte per point"};
+const char* kDescriptions[kNumMethods] = {
     "Batched atomicMin rasterizer over the 10-10-10 bit encoded layout; each batch picks 10, 20 "
     "or 30 bit coordinates from its projected size; point-index payload.",
     "Same algorithm reading four consecutive points per 128-bit load.",
     "High-quality shading: depth pass, then averaging of all points within 1% of the nearest "
     "depth.",
-    "Plain 16 byte per point layout, one 64-bit atomicMin of depth|color per point."};
+    "Plain 16 byte per point layout, one 64-bit atomicMin of depth|color per point.",
+    "Plain 16 byte per point layout; the points of a warp are partitioned by pixel and only each "
+    "partition's closest point is written (depth<<24|color).",
+    "Plain 16 byte per point layout; a warp on one pixel writes only its closest point, otherwise "
+    "pairs of lanes drop the farther of two points on one pixel (depth<<24|color)."};
+
+bool plain_method(int32_t m) {
+    return m == CR_METHOD_EARLYZ || m == CR_METHOD_DEDUP || m == CR_METHOD_EARLYZ_REDUCE;
+}
 
 int default_quirks(int32_t method) {
     switch (method) {
@@ -274,13 +286,15 @@ const char* cr_status_string(cr_status s) {
     return "unknown status";
 }
 
-const char* cr_method_name(int32_t m) { return (m >= 0 && m < 4) ? kNames[m] : nullptr; }
-const char* cr_method_group(int32_t m) { return (m >= 0 && m < 4) ? kGroups[m] : nullptr; }
-const char* cr_method_description(int32_t m) { return (m >= 0 && m < 4) ? kDescriptions[m] : nullptr; }
+const char* cr_method_name(int32_t m) { return (m >= 0 && m < kNumMethods) ? kNames[m] : nullptr; }
+const char* cr_method_group(int32_t m) { return (m >= 0 && m < kNumMethods) ? kGroups[m] : nullptr; }
+const char* cr_method_description(int32_t m) {
+    return (m >= 0 && m < kNumMethods) ? kDescriptions[m] : nullptr;
+}
 
 cr_status cr_method_find(const char* name, int32_t* method) {
     if (!name || !method) return CR_ERR_INVALID_ARG;
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < kNumMethods; i++)
         if (std::strcmp(name, kNames[i]) == 0) {
             *method = i;
             return CR_OK;
@@ -297,7 +311,7 @@ void cr_render_params_default(int32_t method, cr_render_params* out) {
     out->frustum_culling = 1;
     out->resolve = 1;
     out->clear_after = 1;
-    out->clear_value = method == CR_METHOD_EARLYZ ? kPlainReclear : kDefaultClear;
+    out->clear_value = plain_method(method) ? kPlainReclear : kDefaultClear;
 }
 
 // ---- context ----------------------------------------------------------------
@@ -627,7 +641,7 @@ cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params*
         rc = launch_resolve_hqs(fb->W, fb->H, fb->depth, fb->accum, fb->image, p->clear_after, stream);
     } else {
         if (fb->kind != CR_FB_U64) return fail(ctx, CR_ERR_INVALID_ARG, "method needs a u64 fb%s", "");
-        if (p->method == CR_METHOD_EARLYZ) {
+        if (plain_method(p->method)) {
             rc = launch_resolve_plain(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value, stream);
         } else if (p->payload == CR_PAYLOAD_COLOR) {
             rc = launch_resolve_color(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value, stream);
@@ -645,20 +659,20 @@ cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params*
 cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
                     const cr_render_params* p, cr_fb* fb, void* stream) {
     if (!ctx || !cloud || !view || !p || !fb) return CR_ERR_INVALID_ARG;
-    if (p->method < 0 || p->method > CR_METHOD_EARLYZ)
+    if (p->method < 0 || p->method >= kNumMethods)
         return fail(ctx, CR_ERR_INVALID_ARG, "unknown method %s%lld", "", (long long)p->method);
     if (view->width != fb->W || view->height != fb->H)
         return fail(ctx, CR_ERR_INVALID_ARG, "view size differs from the framebuffer%s", "");
     cr_status s = check_size(ctx, view->width, view->height);
     if (s != CR_OK) return s;
     const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? default_quirks(p->method) : p->quirks;
-    const bool plain = p->method == CR_METHOD_EARLYZ;
+    const bool plain = plain_method(p->method);
     const bool hqs = p->method == CR_METHOD_LOOP_LAS_HQS;
 
     // ---- validation before anything is enqueued
     if (plain) {
-        if (!cloud->plain) return fail(ctx, CR_ERR_INVALID_ARG, "early-z needs a plain cloud%s", "");
-        if (fb->kind != CR_FB_U64) return fail(ctx, CR_ERR_INVALID_ARG, "early-z needs a u64 fb%s", "");
+        if (!cloud->plain) return fail(ctx, CR_ERR_INVALID_ARG, "2021 methods need a plain cloud%s", "");
+        if (fb->kind != CR_FB_U64) return fail(ctx, CR_ERR_INVALID_ARG, "2021 methods need a u64 fb%s", "");
         if (!finite_all(view->view, 16) || !finite_all(view->proj, 16))
             return fail(ctx, CR_ERR_INVALID_ARG, "view matrices must be finite%s", "");
     } else {
@@ -693,7 +707,8 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
         mat_mul(pv, id, T);
         mark(1, -1);
         const int grid = ctx->num_sms * 8;
-        if (launch_plain(T, fb->W, fb->H, cloud->verts, cloud->n, fb->fb, grid, stream) != 0)
+        const int variant = p->method == CR_METHOD_DEDUP ? 1 : (p->method == CR_METHOD_EARLYZ_REDUCE ? 2 : 0);
+        if (launch_plain(T, fb->W, fb->H, cloud->verts, cloud->n, fb->fb, grid, variant, stream) != 0)
             return fail(ctx, CR_ERR_CUDA, "plain raster launch failed%s", "");
         mark(2, CR_STAGE_RASTER);
         mark(3, -1);
@@ -707,6 +722,7 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
 
     ViewParams vp;
     s = build_view_params(ctx, cloud, view, p->frustum_culling, &vp);
+    vp.lod_skip_level = p->lod_skip_level;
     if (s != CR_OK) return s;
     int64_t nb = cloud->nb;
     if (quirks & CR_QUIRK_DISPATCH_BY_POINTS)

@@ -37,6 +37,7 @@ struct ViewParams {
     int32_t W, H;
     int32_t nfiles;
     int32_t culling;
+    int32_t lod_skip_level;  // >0: batches at level >= this are not rendered
     FileRec files[kInlineFiles];
 };
 
@@ -80,8 +81,9 @@ int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb_dispat
                 int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream);
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
                    void* stream);
+// variant 0: early-z, 1: dedup, 2: early-z & reduce (the three plain methods)
 int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
-                 uint64_t* fb, int grid, void* stream);
+                 uint64_t* fb, int grid, int variant, void* stream);
 int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgba,
                          int64_t rgba_words, uint32_t* image, int clear_after, uint64_t clear,
                          void* stream);
@@ -146,6 +148,7 @@ struct MVFrame {
     uint32_t* images;
     uint32_t* scratch;       // mv_scratch_words(ci.nb, nviews) words
     int32_t G, block, ctas_per_sm, quirks, payload, culling, num_sms;
+    int32_t lod_skip_level;  // >0: a view skips batches at its level >= this
     int32_t clear_before;    // fill every view's W*H+W+1 words with clear_value first
     int32_t resolve, clear_after;
     uint64_t clear_value;

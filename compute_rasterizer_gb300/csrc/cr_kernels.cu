@@ -58,7 +58,8 @@ __global__ void __launch_bounds__(256) k_cull(ViewParams vp, const cr_batch* __r
             bool vis = !vp.culling || intersects_frustum(f.planes, mnx, mny, mnz, mxx, mxy, mxz);
             if (vis) {
                 int level = precision_level(vp.P, f.VW, vp.W, vp.H, mnx, mny, mnz, mxx, mxy, mxz);
-                keep = true;
+                // compute_loop_nodes/render.cs:273-276: the level-of-detail cut
+                keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 item = (uint32_t)b | ((uint32_t)level << 29);
             }
         }
@@ -306,7 +307,16 @@ struct PlainParams {
     int32_t W, H;
 };
 
-template <int BLOCK>
+// VARIANT 0: compute_2021_earlyz/render.cs:35-74, key depth << 32 | color
+//   through the CTA z-cache.
+// VARIANT 1, 2: compute_2021_dedup/render.cs:33-69 and
+//   compute_2021_earlyz_reduce/render.cs:44-82.  A warp is 32 consecutive
+//   points (the grid stride is a multiple of 32), the reference's subgroup;
+//   lanes whose point is outside the view are not part of the reduction.
+//   key = depth << 24 | color, the color's top byte overlapping the low depth
+//   byte as in the reference, so the reduction decides which keys reach the
+//   framebuffer.  Writers read the word first and atomicMin if smaller.
+template <int BLOCK, int VARIANT>
 __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __restrict__ v,
                                                  int64_t n, uint64_t* __restrict__ fb) {
     BatchCtx c;
@@ -317,9 +327,11 @@ __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __
     c.Wf = (float)pp.W; c.Hf = (float)pp.H; c.W = pp.W;
     BatchedLaunch bl{};
     bl.fb = fb;
-    __shared__ unsigned long long s_zc[kZCacheSlots];
-    for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
-    __syncthreads();
+    __shared__ unsigned long long s_zc[VARIANT == 0 ? kZCacheSlots : 1];
+    if (VARIANT == 0) {
+        for (int i = threadIdx.x; i < kZCacheSlots; i += BLOCK) s_zc[i] = 0xFFFFFFFFull;
+        __syncthreads();
+    }
     const int64_t stride = (int64_t)gridDim.x * BLOCK;
     for (int64_t base = (int64_t)blockIdx.x * BLOCK; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
@@ -330,7 +342,35 @@ __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __
         uint32_t wbits;
         const bool ok = project(c, __uint_as_float(p.x), __uint_as_float(p.y), __uint_as_float(p.z),
                                 pix, wbits) && act;
-        Emit<kModeRaster>::run(bl, s_zc, ok, pix, wbits, p.w, 0u);
+        if (VARIANT == 0) {
+            Emit<kModeRaster>::run(bl, s_zc, ok, pix, wbits, p.w, 0u);
+            continue;
+        }
+        // wbits = floatBitsToInt(pos.w), positive for every point in view
+        bool write;
+        if (VARIANT == 1) {
+            // subgroupPartitionNV(pixelID) + subgroupPartitionedMinNV(depth)
+            const uint32_t peers = __match_any_sync(kFull, ok ? (uint32_t)pix : kNoPixel);
+            const uint32_t mind = __reduce_min_sync(peers, ok ? wbits : 0xFFFFFFFFu);
+            write = ok && wbits == mind;
+        } else {
+            const uint32_t active = __ballot_sync(kFull, ok);
+            const int first = active ? __ffs(active) - 1 : 0;
+            const int32_t first_pix = __shfl_sync(kFull, pix, first);
+            // subgroupAllEqual(pixelID) over the active lanes
+            const bool same = __all_sync(kFull, !ok || pix == first_pix);
+            const uint32_t mind = __reduce_min_sync(kFull, ok ? wbits : 0xFFFFFFFFu);
+            // pair partner (lane ^ 1): subgroupClusteredXor / ClusteredMin over 2
+            const int32_t q_pix = __shfl_xor_sync(kFull, pix, 1);
+            const uint32_t q_depth = __shfl_xor_sync(kFull, wbits, 1);
+            const bool q_ok = (active >> (lane_id() ^ 1u)) & 1u;
+            write = ok && (same ? wbits == mind : (!q_ok || q_pix != pix || wbits <= q_depth));
+        }
+        if (write) {
+            const unsigned long long key = ((unsigned long long)wbits << 24) | p.w;
+            unsigned long long* w = reinterpret_cast<unsigned long long*>(fb) + pix;
+            if (key < *reinterpret_cast<volatile unsigned long long*>(w)) atomicMin(w, key);
+        }
     }
 }
 
@@ -539,7 +579,7 @@ int batched_blocks_per_sm(int mode, int payload, int block) {
 }
 
 int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
-                 uint64_t* fb, int grid, void* stream) {
+                 uint64_t* fb, int grid, int variant, void* stream) {
     if (n <= 0) return 0;
     PlainParams pp;
     for (int i = 0; i < 16; i++) pp.T[i] = T[i];
@@ -547,7 +587,11 @@ int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, in
     pp.H = H;
     int64_t need = (n + 255) / 256;
     if (need < grid) grid = (int)need;
-    k_plain<256><<<grid, 256, 0, (cudaStream_t)stream>>>(pp, reinterpret_cast<const uint4*>(v), n, fb);
+    const uint4* v4 = reinterpret_cast<const uint4*>(v);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (variant == 1) k_plain<256, 1><<<grid, 256, 0, s>>>(pp, v4, n, fb);
+    else if (variant == 2) k_plain<256, 2><<<grid, 256, 0, s>>>(pp, v4, n, fb);
+    else k_plain<256, 0><<<grid, 256, 0, s>>>(pp, v4, n, fb);
     return launch_status();
 }
 

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(256) k_mv_cull(const MVView* __restrict__ view
                                                  int32_t nfiles, int32_t G, int32_t ngroups,
                                                  const cr_batch* __restrict__ batches, int64_t nb,
                                                  int64_t capacity, int32_t quirks, int32_t culling,
+                                                 int32_t lod_skip_level,
                                                  uint32_t* __restrict__ scratch) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
@@ -75,6 +76,7 @@ __global__ void __launch_bounds__(256) k_mv_cull(const MVView* __restrict__ view
                 const MVView& vw = views[v];
                 if (culling && !intersects_frustum(f.planes, mnx, mny, mnz, mxx, mxy, mxz)) continue;
                 const int level = precision_level(vw.P, f.VW, vw.W, vw.H, mnx, mny, mnz, mxx, mxy, mxz);
+                if (lod_skip_level > 0 && level >= lod_skip_level) continue;  // nodes/render.cs:273
                 vismask |= 1u << s;
                 levels |= (uint32_t)level << (3 * s);
             }
@@ -453,7 +455,7 @@ cr_status mv_enqueue(const MVFrame& f, void* stream, const char** what) {
     if (threads > 0) {
         k_mv_cull<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
             f.d_views, f.d_files, f.nviews, f.ci.nfiles, G, ngroups, f.ci.batches, nb,
-            f.ci.capacity, f.quirks, f.culling, f.scratch);
+            f.ci.capacity, f.quirks, f.culling, f.lod_skip_level, f.scratch);
         if (cudaGetLastError() != cudaSuccess) return fail("cull launch");
         MVArgs a;
         a.views = f.d_views;
@@ -582,6 +584,7 @@ cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
     f.quirks = mv->quirks;
     f.payload = p.payload;
     f.culling = p.frustum_culling;
+    f.lod_skip_level = p.lod_skip_level;
     f.num_sms = mv->num_sms;
     f.clear_before = 0;
     f.resolve = p.resolve;

@@ -70,6 +70,7 @@ extern "C" cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_
     cr::ViewParams vp;
     s = cr::view_params_for(view, box_min, num_files, p->frustum_culling, &vp);
     if (s != CR_OK) return s;
+    vp.lod_skip_level = p->lod_skip_level;
     const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT
                            ? (p->method == CR_METHOD_LOOP_LAS
                                   ? CR_QUIRK_L0_X12

@@ -47,12 +47,15 @@ typedef enum cr_status {
 } cr_status;
 
 /* Method ids; names as registered by the reference (compute_loop_las.h:82,
- * compute_loop_las2.h:82, compute_loop_las_hqs.h:88, compute_2021_earlyz.h:52). */
+ * compute_loop_las2.h:82, compute_loop_las_hqs.h:88, compute_2021_earlyz.h:52,
+ * compute_2021_dedup.h:52, compute_2021_earlyz_reduce.h:52). */
 typedef enum cr_method {
     CR_METHOD_LOOP_LAS = 0,          /* "loop_las" */
     CR_METHOD_LOOP_LAS_PREFETCH = 1, /* "loop_las_prefetch" */
     CR_METHOD_LOOP_LAS_HQS = 2,      /* "loop_las_hqs" */
-    CR_METHOD_EARLYZ = 3             /* "(2021) early-z" */
+    CR_METHOD_EARLYZ = 3,            /* "(2021) early-z" */
+    CR_METHOD_DEDUP = 4,             /* "(2021) dedup" */
+    CR_METHOD_EARLYZ_REDUCE = 5      /* "(2021) early-z & reduce" */
 } cr_method;
 
 typedef enum cr_payload {
@@ -106,7 +109,10 @@ typedef struct cr_render_params {
     int32_t block_threads;   /* threads per CTA for the batched kernels; 0 = tuned default */
     int32_t ctas_per_sm;     /* persistent CTAs per SM; 0 = tuned default */
     int32_t views_per_group; /* multi-view: views sharing one point fetch; 0 = tuned default */
-    int32_t reserved[5];
+    int32_t lod_skip_level;  /* >0: skip batches whose precision level is >= this, the level-of-
+                                detail cut of compute_loop_nodes/render.cs:273-276 (which uses 4);
+                                0 = render every visible batch, as the loop_las methods do */
+    int32_t reserved[4];
 } cr_render_params;
 
 typedef struct cr_ctx cr_ctx;

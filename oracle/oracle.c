@@ -377,6 +377,7 @@ static void raster_range(const raster_job* j) {
         float wmax[3] = {b->max_x, b->max_y, b->max_z};
         if (fr->frustum_culling && !or_intersects_frustum(file->planes, wmin, wmax)) continue;
         int level = or_precision_level(fr, file, wmin, wmax);
+        if (fr->lod_skip_level > 0 && level >= fr->lod_skip_level) continue;
         batch_decode d;
         make_decode(b, level, &d);
         int64_t count = or_points_in_batch(b, fr->quirks);
@@ -465,8 +466,10 @@ void or_hqs_depth(const or_frame* fr, const or_batch* batches, int64_t num_batch
         float wmin[3] = {b->min_x, b->min_y, b->min_z};
         float wmax[3] = {b->max_x, b->max_y, b->max_z};
         if (fr->frustum_culling && !or_intersects_frustum(file->planes, wmin, wmax)) continue;
+        const int level = or_precision_level(fr, file, wmin, wmax);
+        if (fr->lod_skip_level > 0 && level >= fr->lod_skip_level) continue;
         batch_decode d;
-        make_decode(b, or_precision_level(fr, file, wmin, wmax), &d);
+        make_decode(b, level, &d);
         int64_t count = or_points_in_batch(b, fr->quirks);
         for (int64_t l = 0; l < count; l++) {
             int64_t idx = (int64_t)b->first_point + l;
@@ -493,8 +496,10 @@ void or_hqs_color(const or_frame* fr, const or_batch* batches, int64_t num_batch
         float wmin[3] = {b->min_x, b->min_y, b->min_z};
         float wmax[3] = {b->max_x, b->max_y, b->max_z};
         if (fr->frustum_culling && !or_intersects_frustum(file->planes, wmin, wmax)) continue;
+        const int level = or_precision_level(fr, file, wmin, wmax);
+        if (fr->lod_skip_level > 0 && level >= fr->lod_skip_level) continue;
         batch_decode d;
-        make_decode(b, or_precision_level(fr, file, wmin, wmax), &d);
+        make_decode(b, level, &d);
         int64_t count = or_points_in_batch(b, fr->quirks);
         for (int64_t l = 0; l < count; l++) {
             int64_t idx = (int64_t)b->first_point + l;
@@ -552,6 +557,67 @@ void or_raster_plain(const float T[16], int32_t W, int32_t H, const or_vertex* v
         if (!project(T, W, H, p, &pix, &w)) continue;
         uint64_t key = ((uint64_t)f2u(w) << 32) | v[i].color;
         if (key < fb[pix]) fb[pix] = key;
+    }
+}
+
+/* The two warp-reduction variants of the plain path, over subgroups of 32
+ * consecutive points (gl_SubgroupSize on the reference's GPU; a subgroup op
+ * sees only the invocations that did not return at the culling test).  Both
+ * pack key = depth << 24 | color, the color's top byte overlapping the low
+ * depth byte, so which points reach the atomic decides the result.
+ *   variant 1: compute_2021_dedup/render.cs:33-69 -- partition by pixel id,
+ *     lanes at their partition's minimum depth write.
+ *   variant 2: compute_2021_earlyz_reduce/render.cs:44-82 -- if every active
+ *     lane has the same pixel, only the subgroup's minimum depth writes;
+ *     otherwise a lane writes unless its pair partner (lane ^ 1) is active, on
+ *     the same pixel and strictly closer.
+ * Points past n are not active (the reference reads past the bound range). */
+void or_raster_plain_warp(const float T[16], int32_t W, int32_t H, const or_vertex* v, int64_t n,
+                          uint64_t* fb, int32_t variant) {
+    for (int64_t w0 = 0; w0 < n; w0 += 32) {
+        int ok[32], write[32];
+        int32_t pix[32];
+        uint32_t depth[32];
+        for (int l = 0; l < 32; l++) {
+            const int64_t i = w0 + l;
+            ok[l] = 0;
+            write[l] = 0;
+            pix[l] = 0;
+            depth[l] = 0;
+            if (i >= n) continue;
+            float p[3] = {v[i].x, v[i].y, v[i].z}, w;
+            ok[l] = project(T, W, H, p, &pix[l], &w);
+            depth[l] = f2u(w);
+        }
+        if (variant == 1) {
+            for (int l = 0; l < 32; l++) {
+                if (!ok[l]) continue;
+                uint32_t mind = depth[l];
+                for (int m = 0; m < 32; m++)
+                    if (ok[m] && pix[m] == pix[l] && depth[m] < mind) mind = depth[m];
+                write[l] = depth[l] == mind;
+            }
+        } else {
+            int first = -1, same = 1;
+            uint32_t mind = 0xFFFFFFFFu;
+            for (int l = 0; l < 32; l++) {
+                if (!ok[l]) continue;
+                if (first < 0) first = l;
+                else if (pix[l] != pix[first]) same = 0;
+                if (depth[l] < mind) mind = depth[l];
+            }
+            for (int l = 0; l < 32; l++) {
+                if (!ok[l]) continue;
+                const int q = l ^ 1;
+                if (same) write[l] = depth[l] == mind;
+                else write[l] = !ok[q] || pix[q] != pix[l] || depth[l] <= depth[q];
+            }
+        }
+        for (int l = 0; l < 32; l++) {
+            if (!write[l]) continue;
+            const uint64_t key = ((uint64_t)depth[l] << 24) | v[w0 + l].color;
+            if (key < fb[pix[l]]) fb[pix[l]] = key;
+        }
     }
 }
 

@@ -84,6 +84,8 @@ typedef struct or_frame {
     int32_t frustum_culling;
     int32_t quirks;
     int32_t payload;
+    int32_t lod_skip_level; /* >0: skip batches at precision level >= this
+                               (compute_loop_nodes/render.cs:273-276 uses 4) */
     int32_t num_files;
     const or_file_frame* files;
 } or_frame;
@@ -136,6 +138,10 @@ void or_hqs_resolve(int32_t width, int32_t height, const uint64_t* accum, uint32
 void or_plain_transform(const double view[16], const double proj[16], float out[16]);
 void or_raster_plain(const float transform[16], int32_t width, int32_t height,
                      const or_vertex* v, int64_t n, uint64_t* fb);
+/* compute_2021_dedup (variant 1) / compute_2021_earlyz_reduce (variant 2):
+ * warp reductions over 32 consecutive points, key depth << 24 | color. */
+void or_raster_plain_warp(const float T[16], int32_t W, int32_t H, const or_vertex* v, int64_t n,
+                          uint64_t* fb, int32_t variant);
 void or_resolve_plain(int32_t width, int32_t height, uint64_t* fb, uint8_t* out_rgba8,
                       uint64_t reclear);
 

@@ -27,7 +27,8 @@ class FileFrame(C.Structure):
 class Frame(C.Structure):
     _fields_ = [("proj", C.c_float * 16), ("width", C.c_int32), ("height", C.c_int32),
                 ("frustum_culling", C.c_int32), ("quirks", C.c_int32), ("payload", C.c_int32),
-                ("num_files", C.c_int32), ("files", C.POINTER(FileFrame))]
+                ("lod_skip_level", C.c_int32), ("num_files", C.c_int32),
+                ("files", C.POINTER(FileFrame))]
 
 
 def build() -> None:
@@ -56,6 +57,7 @@ def lib() -> C.CDLL:
             "or_hqs_resolve": [I32, I32, P, P],
             "or_plain_transform": [P, P, P],
             "or_raster_plain": [P, I32, I32, P, I64, P],
+            "or_raster_plain_warp": [P, I32, I32, P, I64, P, I32],
             "or_resolve_plain": [I32, I32, P, P, C.c_uint64],
             "or_encode_las": [P, I64, I32, I32, P, P, P, I64, I32, P, P, P, P, P],
             "or_encode_standard": [P, I64, I32, I32, P, P, P, P],
@@ -105,7 +107,7 @@ def fnv(a: np.ndarray) -> int:
     return int(lib().or_fnv1a64(_p(a), a.nbytes))
 
 
-def make_frame(view, proj, width, height, box_mins, culling=1, quirks=0, payload=0):
+def make_frame(view, proj, width, height, box_mins, culling=1, quirks=0, payload=0, lod_skip_level=0):
     """Frame + per-file records from double matrices (compute_loop_las.h:141-200)."""
     o = lib()
     view = np.ascontiguousarray(view, np.float64).reshape(16)
@@ -119,6 +121,7 @@ def make_frame(view, proj, width, height, box_mins, culling=1, quirks=0, payload
     o.or_proj_float(_p(proj), C.cast(fr.proj, C.c_void_p))
     fr.width, fr.height = int(width), int(height)
     fr.frustum_culling, fr.quirks, fr.payload = int(culling), int(quirks), int(payload)
+    fr.lod_skip_level = int(lod_skip_level)
     fr.num_files = len(box_mins)
     fr.files = files
     fr._keep = files
@@ -178,14 +181,18 @@ def hqs(frame, batches, n, low, med, hig, rgba):
 
 
 def plain(view, proj, width, height, vertices, clear=0xFFFFFFFFFFFFFFFF,
-          reclear=0xFFFFFFFFFF3C321E):
+          reclear=0xFFFFFFFFFF3C321E, variant=0):
+    """The plain 16 B path: variant 0 early-z, 1 dedup, 2 early-z & reduce."""
     T = np.empty(16, np.float32)
     view = np.ascontiguousarray(view, np.float64).reshape(16)
     proj = np.ascontiguousarray(proj, np.float64).reshape(16)
     lib().or_plain_transform(_p(view), _p(proj), _p(T))
     fb = np.full(fb_words(width, height), clear, dtype=np.uint64)
     v = np.ascontiguousarray(vertices)
-    lib().or_raster_plain(_p(T), width, height, _p(v), len(v), _p(fb))
+    if variant == 0:
+        lib().or_raster_plain(_p(T), width, height, _p(v), len(v), _p(fb))
+    else:
+        lib().or_raster_plain_warp(_p(T), width, height, _p(v), len(v), _p(fb), int(variant))
     fb_before = fb.copy()
     img = np.empty(width * height, dtype=np.uint32)
     lib().or_resolve_plain(width, height, _p(fb), _p(img), reclear)

@@ -22,7 +22,8 @@ static int fail(const char* what, cr_status s) {
 }
 
 int main(int argc, char** argv) {
-    const char* names[] = {"loop_las", "loop_las_prefetch", "loop_las_hqs", "(2021) early-z"};
+    const char* names[] = {"loop_las",       "loop_las_prefetch", "loop_las_hqs",
+                           "(2021) early-z", "(2021) dedup",      "(2021) early-z & reduce"};
     if (argc == 2 && std::strcmp(argv[1], "info") == 0) {
         for (const char* n : names) {
             std::string name, group, desc;

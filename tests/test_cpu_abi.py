@@ -79,3 +79,14 @@ def test_no_gpu_context_fails_cleanly():
     lib = L.load()
     h = C.c_void_p()
     assert lib.cr_ctx_create(0, C.byref(h)) == L.CUDA_ERROR and not h.value
+
+
+def test_bench_workloads_are_defined():
+    """Every workload bench.py runs after the headline frame is defined (the
+    extras run on a GPU only, so a missing one would show up there late)."""
+    import ast
+    src = (ROOT / "bench.py").read_text()
+    defined = {n.name for n in ast.parse(src).body if isinstance(n, ast.FunctionDef)}
+    for fn in ("extras", "multiview_64", "small_configs", "serving", "e2e", "cpu_baseline",
+               "reference_arm", "main"):
+        assert fn in defined, fn

@@ -12,7 +12,8 @@ def test_adapter_reports_registered_methods(tmp_path):
     assert res.returncode == 0, res.stderr
     lib = L.load()
     want = []
-    for m in (L.METHOD_LOOP_LAS, L.METHOD_LOOP_LAS_PREFETCH, L.METHOD_LOOP_LAS_HQS, L.METHOD_EARLYZ):
+    for m in (L.METHOD_LOOP_LAS, L.METHOD_LOOP_LAS_PREFETCH, L.METHOD_LOOP_LAS_HQS, L.METHOD_EARLYZ,
+              L.METHOD_DEDUP, L.METHOD_EARLYZ_REDUCE):
         want.append("|".join(x.decode() for x in (lib.cr_method_name(m), lib.cr_method_group(m),
                                                    lib.cr_method_description(m))))
     assert res.stdout.splitlines() == want

@@ -200,3 +200,88 @@ def test_golden_vectors():
             continue
         got = G.run_case(case)
         assert got == case["digests"], case["name"]
+
+
+def _warp_scene(seed=4, warps=48, W=64, H=32):
+    """Points whose pixel and depth are known: w = z exactly, x and y placed
+    so that x / w lands on pixel centres.  Few pixels, so warps collide;
+    negative z culls a lane."""
+    rng = np.random.default_rng(seed)
+    n = 32 * warps - 5  # a partial last warp
+    v = np.zeros(n, dtype=L.VERTEX_DTYPE)
+    px = rng.integers(0, 2, n)
+    py = rng.integers(0, 2, n)
+    # depths that differ in their low mantissa byte, where the color's top
+    # byte lands in the key; x / w stays deep inside the chosen pixel
+    zs = np.array([1.0 + k * 2.0**-23 for k in range(6)] + [2.0, -2.0], dtype=np.float32)
+    z = rng.choice(zs, n).astype(np.float64)
+    v["x"] = ((px + 0.5) * 2.0 / W - 1.0) * np.abs(z)
+    v["y"] = ((py + 0.5) * 2.0 / H - 1.0) * np.abs(z)
+    v["z"] = z
+    v["color"] = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    proj = np.zeros(16)
+    proj[0] = proj[5] = proj[10] = 1.0
+    proj[11] = 1.0  # w = z (column-major: row 3, column 2)
+    return v, np.eye(4).reshape(16), proj, W, H, px + py * W
+
+
+def _warp_reference(v, pix, variant, words):
+    fb = np.full(words, 0xFFFFFFFFFFFFFFFF, dtype=np.uint64)
+    depth = v["z"].astype(np.float32).view(np.uint32).astype(np.int64)
+    ok = v["z"] > 0
+    for w0 in range(0, len(v), 32):
+        lanes = range(w0, min(w0 + 32, len(v)))
+        act = [i for i in lanes if ok[i]]
+        write = set()
+        if variant == 0:
+            write = set(act)
+        elif variant == 1:
+            for i in act:
+                write.add(i) if depth[i] == min(depth[j] for j in act if pix[j] == pix[i]) else None
+        else:
+            same = len({pix[i] for i in act}) <= 1
+            mind = min((depth[i] for i in act), default=None)
+            for i in act:
+                q = w0 + ((i - w0) ^ 1)
+                q_ok = q < len(v) and ok[q]
+                if (same and depth[i] == mind) or (not same and (not q_ok or pix[q] != pix[i]
+                                                                 or depth[i] <= depth[q])):
+                    write.add(i)
+        for i in write:
+            key = np.uint64((int(depth[i]) << 24) | int(v["color"][i]))
+            fb[pix[i]] = min(fb[pix[i]], key)
+    return fb
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_plain_warp_variants_oracle_semantics(variant):
+    """The oracle's dedup / early-z & reduce warp rules against a plain Python
+    restatement on a scene with exact pixels and depths."""
+    v, view, proj, W, H, pix = _warp_scene()
+    got, _, _ = O.plain(view, proj, W, H, v, variant=variant)
+    want = _warp_reference(v, pix, variant, O.fb_words(W, H))
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_plain_warp_variants_keep_the_closer_point(variant):
+    """Lanes 0 and 1 on one pixel: lane 0 closer but with color alpha 0xFF,
+    lane 1 one ulp farther with alpha 0, so lane 1's depth << 24 | color key
+    is the smaller one; lane 2 on another pixel.  Both reductions drop lane 1
+    before the atomic, so the pixel keeps lane 0's key."""
+    v, view, proj, W, H, _ = _warp_scene()
+    v = v[:3].copy()
+    d0 = np.float32(1.0)
+    d1 = np.nextafter(d0, np.float32(2.0))
+    for i, (px, z, color) in enumerate([(5, d0, 0xFF102030), (5, d1, 0x00405060), (9, d0, 0x7F000001)]):
+        v["z"][i] = z
+        v["x"][i] = ((px + 0.5) * 2.0 / W - 1.0) * float(z)
+        v["y"][i] = (0.5 * 2.0 / H - 1.0) * float(z)
+        v["color"][i] = color
+    got, _, _ = O.plain(view, proj, W, H, v, variant=variant)
+    key0 = (int(d0.view(np.uint32)) << 24) | 0xFF102030
+    key1 = (int(d1.view(np.uint32)) << 24) | 0x00405060
+    assert key1 < key0
+    assert int(got[5]) == key0
+    every, _, _ = O.plain(view, proj, W, H, v, variant=0)
+    assert int(every[5]) >> 32 == int(d0.view(np.uint32))  # early-z: depth << 32 keeps lane 0 too

@@ -126,3 +126,23 @@ def test_autotune_keeps_output_identical(ctx, scene):
         want, _ = single_view(ctx, cloud, cams[i], L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX)
         assert np.array_equal(mv.read(i, L.FB_WORDS), want), i
     mv.close()
+
+
+def test_multiview_lod_cut_equals_single_views(ctx, scene):
+    """The level-of-detail cut applies per view: every view equals cr_render
+    of that view alone with the same cut."""
+    cl, cloud, cams = scene
+    params = default_params(L.METHOD_LOOP_LAS, payload=L.PAYLOAD_INDEX, views_per_group=8,
+                            resolve=0, clear_after=0, lod_skip_level=3)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    mv.clear()
+    mv.render()
+    ctx.sync()
+    for i, cam in enumerate(cams):
+        fb, _ = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX, lod_skip_level=3)
+        want = fb.read(L.FB_WORDS)
+        got = mv.read(i, L.FB_WORDS)
+        assert np.array_equal(got, want), (i, first_diff(got, want))
+        fb.close()
+    mv.close()

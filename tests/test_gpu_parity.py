@@ -332,3 +332,56 @@ def test_synth_cloud_device_pipeline(ctx):
         fb, _ = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
         want = oracle_fb(cl, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
         assert np.array_equal(fb.read(L.FB_WORDS), want), camname
+
+
+@pytest.mark.parametrize("camname", ["far", "mid"])
+@pytest.mark.parametrize("cut", [4, 3])
+@pytest.mark.parametrize("method", [L.METHOD_LOOP_LAS, L.METHOD_LOOP_LAS_HQS])
+def test_lod_skip_level(ctx, small, camname, cut, method):
+    """compute_loop_nodes/render.cs:273-276: batches at precision level >= the
+    cut are not rendered; the oracle applies the same cut."""
+    cl, cloud = small
+    cam = cameras(cl)[camname]
+    fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[method], O.PAYLOAD_INDEX)
+    fr.lod_skip_level = cut
+    args = (cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+    fb, params = gpu_raw(ctx, cloud, cam, method, L.PAYLOAD_INDEX, lod_skip_level=cut)
+    st = ctx.frame_stats(cloud, params)
+    assert all(st.points_per_level[lv] == 0 for lv in range(cut, 5))
+    if method == L.METHOD_LOOP_LAS_HQS:
+        depth, accum, _ = O.hqs(fr, *args)
+        assert np.array_equal(fb.read(L.FB_DEPTH), depth)
+        assert np.array_equal(fb.read(L.FB_ACCUM), accum)
+    else:
+        want = O.raster_batched(fr, *args)
+        got = fb.read(L.FB_WORDS)
+        assert np.array_equal(got, want), first_diff(got, want)
+        full = oracle_fb(cl, cam, method, L.PAYLOAD_INDEX)
+        if camname == "far":
+            assert not np.array_equal(want, full)  # the cut removed batches
+
+
+@pytest.mark.parametrize("method,variant", [(L.METHOD_DEDUP, 1), (L.METHOD_EARLYZ_REDUCE, 2)])
+@pytest.mark.parametrize("n,w,h", [(100_003, 320, 180), (4_194_304, 1920, 1080), (200_000, 64, 48)])
+def test_plain_warp_variants(ctx, method, variant, n, w, h):
+    """compute_2021_dedup / compute_2021_earlyz_reduce: the warp reductions
+    over 32 consecutive points and the depth << 24 | color packing, bit for
+    bit with the oracle (a partial last warp, the full config-1 scene, and a
+    64x48 view where most of a warp lands on one pixel)."""
+    v = synth.uniform_vertices_host(3, n, 100.0)
+    cloud = ctx.plain_cloud(v)
+    cam = config1_cam(w, h)
+    fb = ctx.framebuffer(w, h)
+    fb.clear(0xFFFFFFFFFFFFFFFF)
+    ctx.render(cloud, make_view(*cam), default_params(method, resolve=0, clear_after=0), fb)
+    got = fb.read(L.FB_WORDS)
+    want, img, recleared = O.plain(cam[0], cam[1], w, h, v, variant=variant)
+    assert np.array_equal(got, want), first_diff(got, want)
+    early, _, _ = O.plain(cam[0], cam[1], w, h, v)
+    assert not np.array_equal(want, early)  # the packing differs from early-z's
+    params = default_params(method)
+    ctx.resolve(cloud, params, fb)
+    assert np.array_equal(fb.read(L.FB_IMAGE), img)
+    assert np.array_equal(fb.read(L.FB_WORDS)[:w * h], recleared[:w * h])
+    fb.close()
+    cloud.close()

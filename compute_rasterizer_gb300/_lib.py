@@ -123,6 +123,7 @@ MAX_POINTS_PER_LOAD = 1024000
 
 SERVE_MAX_POOL_BYTES = 16 << 30
 SERVE_MAX_BATCH_VIEWS = 256
+INJECT_NONE, INJECT_LAUNCH_ALLOC = 0, 1
 
 P = C.c_void_p
 I32, I64, U64, DBL, FLT = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_float
@@ -207,6 +208,7 @@ _SIGS = {
     "cr_server_drain": (I32, [P, I32]),
     "cr_server_replay": (I32, [P, C.POINTER(Request), C.POINTER(DBL), I64, C.POINTER(Completion)]),
     "cr_server_stats_get": (I32, [P, C.POINTER(ServerStats)]),
+    "cr_server_inject": (I32, [P, I32, I32]),
 }
 
 EXPORTED = tuple(_SIGS)

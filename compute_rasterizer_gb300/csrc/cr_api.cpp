@@ -659,6 +659,7 @@ cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params*
 cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
                     const cr_render_params* p, cr_fb* fb, void* stream) {
     if (!ctx || !cloud || !view || !p || !fb) return CR_ERR_INVALID_ARG;
+    const NvtxRange range("cr_render");
     if (p->method < 0 || p->method >= kNumMethods)
         return fail(ctx, CR_ERR_INVALID_ARG, "unknown method %s%lld", "", (long long)p->method);
     if (view->width != fb->W || view->height != fb->H)

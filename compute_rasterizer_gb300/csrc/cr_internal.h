@@ -4,9 +4,21 @@
 
 #include <cstdint>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/cr_raster.h"
 
 namespace cr {
+
+// An NVTX range over a host call (the ranges profilers use to select a
+// frame's launches; free unless a tool is attached).  The reference marks the
+// same spans with GL timestamp queries (GLTimerQueries.cpp:6-22).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 constexpr int kPointsPerBatch = CR_POINTS_PER_BATCH;
 constexpr int kInlineFiles = 8;       // per-file records passed in kernel parameters

@@ -716,6 +716,7 @@ cr_status cr_mv_set_views(cr_mv* mv, const cr_view* views) {
 
 cr_status cr_mv_render(cr_mv* mv, int32_t use_graph, void* stream) {
     if (!mv) return CR_ERR_INVALID_ARG;
+    const NvtxRange range("cr_mv_render");
     if (!mv->views_set) return mv_fail(mv, CR_ERR_INVALID_ARG, "cr_mv_set_views first");
     cudaStream_t st = (cudaStream_t)stream;
     cr_status s = CR_OK;

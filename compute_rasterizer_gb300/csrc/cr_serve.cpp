@@ -140,6 +140,7 @@ struct cr_server {
 
     std::atomic<int32_t> queued{0};
     std::atomic<uint64_t> next_ticket{1};
+    std::atomic<int32_t> inject_alloc_failures{0};  // cr_server_inject
 
     mutable std::mutex stats_mu;
     cr_server_stats stats{};
@@ -234,7 +235,11 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
     // a launch of one request uses the single-view kernels: same image, and
     // faster than the multi-view raster at one view per group
     const bool single = c.plain_launches || n == 1;
-    cudaError_t e = ensure_slot_scratch(sl, cr::mv_scratch_words(nb, single ? 1 : n));
+    int32_t injected = s->inject_alloc_failures.load();
+    while (injected > 0 && !s->inject_alloc_failures.compare_exchange_weak(injected, injected - 1)) {
+    }
+    cudaError_t e = injected > 0 ? cudaErrorMemoryAllocation
+                                 : ensure_slot_scratch(sl, cr::mv_scratch_words(nb, single ? 1 : n));
     if (e != cudaSuccess) {
         *what = "scratch allocation";
         return CR_ERR_OUT_OF_MEMORY;
@@ -385,7 +390,10 @@ bool launch(cr_server* s, Slot& sl, std::deque<Pending>& queue) {
     }
     const char* what = "";
     sl.t_launch = now_us(s);
-    const cr_status st = enqueue(s, sl, ci, &what);
+    const cr_status st = [&] {
+        const cr::NvtxRange range("cr_server launch");
+        return enqueue(s, sl, ci, &what);
+    }();
     if (st != CR_OK) {
         // nothing of this batch is waited for: drain the stream, fail its requests
         set_err(s, st, std::string("launch: ") + what);
@@ -698,6 +706,13 @@ cr_status cr_server_replay(cr_server* s, const cr_request* reqs, const double* a
             got++;
         }
     }
+    return CR_OK;
+}
+
+cr_status cr_server_inject(cr_server* s, int32_t what, int32_t count) {
+    if (!s || count < 0 || (what != CR_INJECT_NONE && what != CR_INJECT_LAUNCH_ALLOC))
+        return CR_ERR_INVALID_ARG;
+    s->inject_alloc_failures.store(what == CR_INJECT_LAUNCH_ALLOC ? count : 0);
     return CR_OK;
 }
 

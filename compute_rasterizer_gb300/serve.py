@@ -114,6 +114,10 @@ class Server:
                     "replay")
         return np.frombuffer(out, dtype=COMPLETION_DTYPE, count=n).copy()
 
+    def inject(self, what: int, count: int):
+        """Host-side fault injection (see cr_server_inject)."""
+        self._check(self.lib.cr_server_inject(self.handle, int(what), int(count)), "inject")
+
     def stats(self) -> dict:
         s = L.ServerStats()
         self._check(self.lib.cr_server_stats_get(self.handle, C.byref(s)), "stats")

@@ -115,6 +115,13 @@ cr_status cr_server_replay(cr_server* s, const cr_request* reqs, const double* a
 
 cr_status cr_server_stats_get(const cr_server* s, cr_server_stats* out);
 
+/* Host-side fault injection for tests: the next `count` launches fail as if
+ * their device allocation had failed (CR_INJECT_LAUNCH_ALLOC), before any
+ * device work; their requests complete with CR_ERR_OUT_OF_MEMORY and the loop
+ * carries on with the next launch.  Nothing faults on the device. */
+enum { CR_INJECT_NONE = 0, CR_INJECT_LAUNCH_ALLOC = 1 };
+cr_status cr_server_inject(cr_server* s, int32_t what, int32_t count);
+
 #ifdef __cplusplus
 }
 #endif

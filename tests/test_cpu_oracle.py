@@ -285,3 +285,74 @@ def test_plain_warp_variants_keep_the_closer_point(variant):
     assert int(got[5]) == key0
     every, _, _ = O.plain(view, proj, W, H, v, variant=0)
     assert int(every[5]) >> 32 == int(d0.view(np.uint32))  # early-z: depth << 32 keeps lane 0 too
+
+
+def test_precision_level_and_frustum_known_answers():
+    """render.cs:199-231 and :176-197 on a scene with a closed-form projected
+    size: a 90-degree camera at the origin looking down -z, 1000x1000 pixels,
+    cubes of side s centred at distance 10, whose centre-to-edge distance on
+    screen is 500 * (s * sqrt(3)) / 10 = 86.6 s pixels."""
+    view = np.eye(4).reshape(16)
+    proj = synth.perspective(90.0, 1.0, 0.1, 1000.0)
+    fr = O.make_frame(view, proj, 1000, 1000, np.zeros((1, 3)))
+    o = O.lib()
+    want = {1.0: 4, 2.0: 3, 4.0: 2, 50.0: 1, 200.0: 0}  # 87, 173, 346, 4330, 17321 px
+    for s, level in want.items():
+        wmin = np.array([-s / 2, -s / 2, -10.0 - s / 2], np.float32)
+        wmax = np.array([s / 2, s / 2, -10.0 + s / 2], np.float32)
+        assert o.or_precision_level(C.byref(fr), C.byref(fr.files[0]), wmin.ctypes.data,
+                                    wmax.ctypes.data) == level, s
+        assert o.or_intersects_frustum(C.cast(fr.files[0].planes, C.c_void_p), wmin.ctypes.data,
+                                       wmax.ctypes.data) == 1
+    behind_min = np.array([-1, -1, 5], np.float32)
+    behind_max = np.array([1, 1, 7], np.float32)
+    assert o.or_intersects_frustum(C.cast(fr.files[0].planes, C.c_void_p), behind_min.ctypes.data,
+                                   behind_max.ctypes.data) == 0
+    beside_min = np.array([40, -1, -11], np.float32)  # x/|z| = 3.6 > 1
+    beside_max = np.array([42, 1, -12], np.float32)
+    assert o.or_intersects_frustum(C.cast(fr.files[0].planes, C.c_void_p), beside_min.ctypes.data,
+                                   beside_max.ctypes.data) == 0
+
+
+@pytest.mark.parametrize("bits", [10, 20, 30])
+def test_encoder_round_trip_bounds(bits):
+    """Quantise -> split -> decode (LasLoaderSparse.cpp:146-198, render.cs:333-397):
+    a decoded coordinate is within size / 2^bits of the original, plus the
+    float rounding of the stored AABB (H8: quantised against the double box,
+    decoded against its float copy)."""
+    n = 30000
+    rec, hdr = synth.las_records_host(synth.synth_params(L.SYNTH_TERRAIN, 300.0, 12), n)
+    batches, lo, md, hi, _ = synth.encode_las(rec, n, hdr)
+    r = rec.reshape(n, 26)
+    X = r[:, 0:12].copy().view("<i4").astype(np.float64)
+    orig = X * np.array(hdr.scale[:]) + np.array(hdr.offset[:]) - np.array(hdr.min[:])
+    for b in batches:
+        sl = slice(int(b["first_point"]), int(b["first_point"]) + int(b["num_points"]))
+        bmin = np.array([b["min_x"], b["min_y"], b["min_z"]], np.float64)
+        bmax = np.array([b["max_x"], b["max_y"], b["max_z"]], np.float64)
+        size = bmax - bmin
+        q = []
+        for k in range(3):
+            w4, w8, w12 = ((s[sl] >> (10 * k)) & 1023 for s in (lo, md, hi))
+            if bits == 10:
+                q.append(w4.astype(np.float64) / 1024.0)
+            elif bits == 20:
+                q.append(((w4.astype(np.int64) << 10) | w8) / 2.0**20)
+            else:
+                q.append(((w4.astype(np.int64) << 20) | (w8.astype(np.int64) << 10) | w12) / 2.0**30)
+        dec = bmin + np.stack(q, axis=1) * size
+        ulp = np.spacing(np.maximum(np.abs(bmin), np.abs(bmax)).astype(np.float32)).astype(np.float64)
+        bound = size / 2.0**bits + 2 * ulp + 1e-12
+        err = np.abs(dec - orig[sl])
+        assert (err <= bound).all(), (bits, float((err - bound).max()))
+
+
+def test_key_packing_orders_by_depth_then_payload():
+    """render.cs:421-423: key = floatBitsToUint(w) << 32 | payload; for w > 0
+    the unsigned key order is the (depth, payload) order."""
+    rng = np.random.default_rng(2)
+    w = rng.uniform(0.01, 1e5, 5000).astype(np.float32)
+    w[::7] = w[1::7][: len(w[::7])]  # ties
+    pay = rng.integers(0, 2**32, 5000, dtype=np.uint64)
+    key = (w.view(np.uint32).astype(np.uint64) << np.uint64(32)) | pay
+    assert np.array_equal(np.argsort(key, kind="stable"), np.lexsort((pay, w)))

@@ -203,3 +203,27 @@ def test_close_finishes_outstanding_requests(ctx, scenes):
     srv.close()  # returns after every accepted request completed
     for i, (c, cam) in enumerate(reqs[:16]):
         assert np.array_equal(images[i], solo_image(ctx, clouds[c], cam, L.PAYLOAD_COLOR, i))
+
+
+def test_injected_launch_failure_does_not_wedge_the_loop(ctx, scenes):
+    """A launch whose (host-simulated) allocation fails completes its requests
+    with OUT_OF_MEMORY; the other requests and every later launch are served."""
+    clouds, reqs = scenes
+    srv = Server(ctx, pool_bytes=64 << 20, max_batch_views=64, max_inflight=1)
+    ids = [srv.add_cloud(c) for c in clouds]
+    srv.inject(L.INJECT_LAUNCH_ALLOC, 1)
+    images, done = serve_all(srv, ids, reqs)
+    failed = [c for c in done if c.status != L.OK]
+    assert len(done) == len(reqs) and failed
+    assert all(c.status == L.OUT_OF_MEMORY for c in failed)
+    assert len({c.t_launch_us for c in failed}) == 1  # one launch failed
+    for c in done:
+        if c.status == L.OK:
+            i = c.user_tag
+            want = solo_image(ctx, clouds[reqs[i][0]], reqs[i][1], L.PAYLOAD_COLOR, i)
+            assert np.array_equal(images[i], want)
+    images, done = serve_all(srv, ids, reqs)
+    assert all(c.status == L.OK for c in done)
+    s = srv.stats()
+    assert s["failed"] == len(failed) and s["pool_used_bytes"] == 0
+    srv.close()

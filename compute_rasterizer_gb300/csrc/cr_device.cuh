@@ -134,8 +134,9 @@ __device__ __forceinline__ uint32_t ld_cached_u32(const uint32_t* p) {
     return v;
 }
 
-// Per-CTA early-z cache in shared memory: a direct-mapped table (Fibonacci
-// hash of a tag) of words `depth << 32 | tag`, where the tag names one
+// Per-CTA early-z cache in shared memory: a direct-mapped table (slot: the
+// tag's low bits for one view, a Fibonacci hash of the tag for several) of
+// words `depth << 32 | tag`, where the tag names one
 // framebuffer word (the pixel id; with several views, the view's word offset
 // plus the pixel id).  Every depth stored is one this CTA submitted to, or read
 // from, the framebuffer during the frame, so it is never below the word's final
@@ -149,6 +150,10 @@ constexpr int kZCacheSlots = 1 << kZCacheBits;
 __device__ __forceinline__ uint32_t zslot(uint32_t tag) {
     return (tag * 2654435761u) >> (32 - kZCacheBits);
 }
+// Single-view slots: a CTA's batch covers a compact screen region, whose pixel
+// ids already differ in their low bits (measured faster than the hash there;
+// the multi-view tags, offset per view, keep the hash).
+__device__ __forceinline__ uint32_t zslot_pixel(uint32_t pix) { return pix & (kZCacheSlots - 1); }
 
 // Writes one point's contribution.  All 32 lanes of the warp call run()
 // together (inactive lanes with ok = false).

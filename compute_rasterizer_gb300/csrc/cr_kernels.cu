@@ -100,7 +100,7 @@ struct Emit<kModeRaster> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long* zc,
                                                bool ok, int32_t pix, uint32_t wbits,
                                                uint32_t payload, uint32_t) {
-        const uint32_t slot = zslot((uint32_t)pix);
+        const uint32_t slot = zslot_pixel((uint32_t)pix);
         // render.cs:423-424 early depth test, against the CTA's cache
         const bool cand = ok && !zcache_rejects(zc, slot, (uint32_t)pix, wbits);
         if (__any_sync(kFull, cand) && cand)
@@ -115,7 +115,7 @@ struct Emit<kModeHqsDepth> {
     static __device__ __forceinline__ void run(const BatchedLaunch& bl, unsigned long long* zc,
                                                bool ok, int32_t pix, uint32_t wbits, uint32_t,
                                                uint32_t) {
-        const uint32_t slot = zslot((uint32_t)pix);
+        const uint32_t slot = zslot_pixel((uint32_t)pix);
         // hqs/depth.cs:375-379
         const bool cand = ok && !zcache_rejects(zc, slot, (uint32_t)pix, wbits);
         if (__any_sync(kFull, cand) && cand)
@@ -148,7 +148,7 @@ __device__ __forceinline__ void hqs_color_flush(const BatchedLaunch& bl, bool ac
 // Points [first, first + count) are read as 128-bit vectors starting at the
 // aligned word below `first`; lanes mask the words outside the range.  The
 // next vector is loaded before the current one is processed.
-template <int MODE, int PAYLOAD, int BLOCK, int LC>
+template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false>
 __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned long long* zc,
                                            const BatchCtx& c, int64_t first, int32_t count,
                                            bool l0_x12) {
@@ -188,7 +188,7 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
         bool run_open = false;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const bool valid = (uint32_t)(rel0 + j) < (uint32_t)count;
+            const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
             const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
             const uint32_t a = u4get(w4, j);
             float x, y, z;
@@ -290,7 +290,10 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
             c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
             c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
             const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-            if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
+            // full, vector-aligned batches (nearly all) skip the per-point range test
+            if (LIST == 0 && count == kPointsPerBatch && (first & 3) == 0)
+                run_points<MODE, PAYLOAD, BLOCK, 2, true>(bl, s_zc, c, first, count, l0_x12);
+            else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
             else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, first, count, l0_x12);
             else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, first, count, l0_x12);
             __syncthreads();

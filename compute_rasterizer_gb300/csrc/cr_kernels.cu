@@ -144,6 +144,33 @@ __device__ __forceinline__ void hqs_color_flush(const BatchedLaunch& bl, bool ac
     }
 }
 
+// Decodes point j of the lane's vector at level class LC (render.cs:333-397).
+template <int LC>
+__device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, const uint4& w12, int j,
+                                             const BatchCtx& c, bool l0_x12, float& x, float& y,
+                                             float& z) {
+    const uint32_t a = u4get(w4, j);
+    if (LC == 2) {
+        x = __fmaf_rn(small_u2f(a & 1023u), c.sx, c.mnx);
+        y = __fmaf_rn(small_u2f((a >> 10) & 1023u), c.sy, c.mny);
+        z = __fmaf_rn(small_u2f((a >> 20) & 1023u), c.sz, c.mnz);
+    } else {
+        const uint32_t b = u4get(w8, j);
+        uint32_t X = ((a & 1023u) << 20) | ((b & 1023u) << 10);
+        uint32_t Y = (((a >> 10) & 1023u) << 20) | (((b >> 10) & 1023u) << 10);
+        uint32_t Z = (((a >> 20) & 1023u) << 20) | (((b >> 20) & 1023u) << 10);
+        if (LC == 0) {
+            const uint32_t h = u4get(w12, j);
+            uint32_t x12 = h & 1023u, y12 = (h >> 10) & 1023u, z12 = (h >> 20) & 1023u;
+            if (l0_x12) { y12 = x12; z12 = x12; }
+            X |= x12; Y |= y12; Z |= z12;
+        }
+        x = __fmaf_rn(__uint2float_rn(X), c.sx, c.mnx);
+        y = __fmaf_rn(__uint2float_rn(Y), c.sy, c.mny);
+        z = __fmaf_rn(__uint2float_rn(Z), c.sz, c.mnz);
+    }
+}
+
 // LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0).
 // Points [first, first + count) are read as 128-bit vectors starting at the
 // aligned word below `first`; lanes mask the words outside the range.  The
@@ -180,63 +207,64 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             if (kNeedColor) ncol = ld_stream(co4 + vn);
         }
         const int32_t rel0 = 4 * v - head;  // batch-local index of word 0
-        // HQS color: the lane's run of consecutive in-view points on one pixel
-        // (Morton order puts most of a lane's 4 points on the same pixel): one
-        // depth read per run, colors summed in registers, one flush per run
-        uint32_t run_pix = kNoPixel, run_rg = 0, run_bc = 0;
-        float run_lim = 0.0f;
-        bool run_open = false;
+        if constexpr (MODE == kModeHqsColor) {
+            // The lane's 4 consecutive points, in runs of in-view points on one
+            // pixel (Morton order puts most of them on the same pixel): project
+            // all 4, read the depth of every run start at once (the reads
+            // overlap; the depth buffer is read-only in this pass), then sum
+            // each run's visible colors and flush it once.
+            int32_t pix[4];
+            uint32_t wb[4];
+            bool ok[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
-            const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
-            const uint32_t a = u4get(w4, j);
-            float x, y, z;
-            if (LC == 2) {
-                x = __fmaf_rn(small_u2f(a & 1023u), c.sx, c.mnx);
-                y = __fmaf_rn(small_u2f((a >> 10) & 1023u), c.sy, c.mny);
-                z = __fmaf_rn(small_u2f((a >> 20) & 1023u), c.sz, c.mnz);
-            } else {
-                const uint32_t b = u4get(w8, j);
-                uint32_t X = ((a & 1023u) << 20) | ((b & 1023u) << 10);
-                uint32_t Y = (((a >> 10) & 1023u) << 20) | (((b >> 10) & 1023u) << 10);
-                uint32_t Z = (((a >> 20) & 1023u) << 20) | (((b >> 20) & 1023u) << 10);
-                if (LC == 0) {
-                    const uint32_t h = u4get(w12, j);
-                    uint32_t x12 = h & 1023u, y12 = (h >> 10) & 1023u, z12 = (h >> 20) & 1023u;
-                    if (l0_x12) { y12 = x12; z12 = x12; }
-                    X |= x12; Y |= y12; Z |= z12;
-                }
-                x = __fmaf_rn(__uint2float_rn(X), c.sx, c.mnx);
-                y = __fmaf_rn(__uint2float_rn(Y), c.sy, c.mny);
-                z = __fmaf_rn(__uint2float_rn(Z), c.sz, c.mnz);
+            for (int j = 0; j < 4; j++) {
+                const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
+                float x, y, z;
+                decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
+                ok[j] = project(c, x, y, z, pix[j], wb[j]) && valid;
             }
-            int32_t pix;
-            uint32_t wbits;
-            const bool ok = project(c, x, y, z, pix, wbits) && valid;
-            const uint32_t color = kNeedColor ? u4get(col, j) : 0u;
-            if constexpr (MODE == kModeHqsColor) {
-                const bool cont = run_open && ok && (uint32_t)pix == run_pix;
-                hqs_color_flush(bl, run_open && !cont && run_bc != 0u, run_pix, run_rg, run_bc);
-                if (ok && !cont) {
-                    // the depth buffer is read-only during this pass
-                    run_pix = (uint32_t)pix;
-                    run_rg = run_bc = 0u;
-                    run_lim = fmul(__uint_as_float(__ldg(bl.depth + pix)), 1.01f);
+            bool cont[4];
+            float lim[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int jp = j > 0 ? j - 1 : 0;
+                cont[j] = j > 0 && ok[jp] && ok[j] && pix[j] == pix[jp];
+                // color.cs:399-403: visible if depth <= bufferDepth * 1.01
+                lim[j] = ok[j] && !cont[j] ? fmul(__uint_as_float(__ldg(bl.depth + pix[j])), 1.01f) : 0.0f;
+            }
+            uint32_t rg = 0u, bc = 0u;
+            float run_lim = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int jp = j > 0 ? j - 1 : 0;
+                if (j > 0) hqs_color_flush(bl, ok[jp] && !cont[j] && bc != 0u, pix[jp], rg, bc);
+                if (!cont[j]) {
+                    rg = bc = 0u;
+                    run_lim = lim[j];
                 }
-                // color.cs:399-403: depth <= bufferDepth * 1.01
-                if (ok && __uint_as_float(wbits) <= run_lim) {
-                    run_rg += (color & 0xFFu) | (((color >> 8) & 0xFFu) << 16);
-                    run_bc += ((color >> 16) & 0xFFu) | (1u << 16);
+                if (ok[j] && __uint_as_float(wb[j]) <= run_lim) {
+                    // R | G << 16 and B | 1 << 16, one byte permute each
+                    const uint32_t color = u4get(col, j);
+                    rg += __byte_perm(color, 0u, 0x4140);
+                    bc += __byte_perm(color, 0x00010000u, 0x7642);
                 }
-                run_open = ok;
-            } else {
+            }
+            hqs_color_flush(bl, ok[3] && bc != 0u, pix[3], rg, bc);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
+                const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
+                float x, y, z;
+                decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
+                int32_t pix;
+                uint32_t wbits;
+                const bool ok = project(c, x, y, z, pix, wbits) && valid;
+                const uint32_t color = kNeedColor ? u4get(col, j) : 0u;
                 const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? color : (uint32_t)idx;
                 Emit<MODE>::run(bl, zc, ok, pix, wbits, payload, color);
             }
         }
-        if constexpr (MODE == kModeHqsColor)
-            hqs_color_flush(bl, run_open && run_bc != 0u, run_pix, run_rg, run_bc);
     }
 }
 

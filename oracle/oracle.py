@@ -132,8 +132,11 @@ def fb_words(width, height) -> int:
     return width * height + width + 1
 
 
-def pad_stream(a, pad=64) -> np.ndarray:
-    """A stream with zeroed words past N (the device streams carry the same)."""
+def pad_stream(a, pad=64, n=None) -> np.ndarray:
+    """A stream with zeroed words past N (the device streams carry the same).
+    A stream that already holds n + pad words is returned as it is."""
+    if n is not None and len(a) >= n + pad:
+        return a
     out = np.zeros(len(a) + pad, dtype=np.uint32)
     out[:len(a)] = a
     return out
@@ -142,8 +145,8 @@ def pad_stream(a, pad=64) -> np.ndarray:
 def raster_batched(frame, batches, n, low, med, hig, rgba, clear=0xFF800000FF800000,
                    threads=1) -> np.ndarray:
     fb = np.full(fb_words(frame.width, frame.height), clear, dtype=np.uint64)
-    low, med, hig = pad_stream(low), pad_stream(med), pad_stream(hig)
-    rgba = pad_stream(rgba) if rgba is not None else None
+    low, med, hig = pad_stream(low, n=n), pad_stream(med, n=n), pad_stream(hig, n=n)
+    rgba = pad_stream(rgba, n=n) if rgba is not None else None
     b = np.ascontiguousarray(batches)
     if threads > 1:
         lib().or_raster_batched_mt(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig),
@@ -170,7 +173,7 @@ def resolve_color(width, height, fb) -> np.ndarray:
 def hqs(frame, batches, n, low, med, hig, rgba):
     depth = np.full(fb_words(frame.width, frame.height), 0xFF800000, dtype=np.uint32)
     accum = np.zeros(2 * fb_words(frame.width, frame.height), dtype=np.uint64)
-    low, med, hig, rgba = (pad_stream(x) for x in (low, med, hig, rgba))
+    low, med, hig, rgba = (pad_stream(x, n=n) for x in (low, med, hig, rgba))
     b = np.ascontiguousarray(batches)
     lib().or_hqs_depth(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig), _p(depth))
     lib().or_hqs_color(C.byref(frame), _p(b), len(b), n, _p(low), _p(med), _p(hig), _p(rgba),

@@ -151,6 +151,7 @@ _SIGS = {
     "cr_cloud_num_points": (I64, [P]),
     "cr_cloud_num_batches": (I64, [P]),
     "cr_cloud_destroy": (I32, [P, P]),
+    "cr_cloud_wrap": (I32, [P, I64, I64, I32, P, P, P, P, P, I64, PP]),
     "cr_cloud_create_plain": (I32, [P, I64, PP]),
     "cr_cloud_upload_plain": (I32, [P, P, P, P]),
     "cr_cloud_device_plain": (I32, [P, PP]),

@@ -47,6 +47,7 @@ struct cr_cloud {
     uint32_t* rgba = nullptr;
     cr_vertex* verts = nullptr;
     std::vector<double> box_min;
+    bool owned = true;  // false: arrays belong to the caller (cr_cloud_wrap)
 };
 
 struct cr_fb {
@@ -439,6 +440,7 @@ cr_status cr_cloud_upload(cr_ctx* ctx, cr_cloud* c, const cr_batch* batches, con
                           const uint32_t* md, const uint32_t* hi, const uint32_t* rgba,
                           const double* box_min, void* stream) {
     if (!ctx || !c || c->plain) return CR_ERR_INVALID_ARG;
+    if (!c->owned) return fail(ctx, CR_ERR_INVALID_ARG, "a wrapped cloud's arrays belong to the caller%s", "");
     cudaStream_t s = (cudaStream_t)stream;
     if (batches) {
         for (int64_t i = 0; i < c->nb; i++) {
@@ -498,7 +500,8 @@ cr_status cr_cloud_read(cr_ctx* ctx, const cr_cloud* c, int32_t which, void* dst
         default: return fail(ctx, CR_ERR_INVALID_ARG, "unknown cloud array %s%lld", "", (long long)which);
     }
     if (!src || bytes > limit) return fail(ctx, CR_ERR_INVALID_ARG, "bad cloud read %s%lld", "", (long long)bytes);
-    CR_CUDA(ctx, cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream),
+    // cudaMemcpyDefault: a wrapped cloud's arrays may be host memory
+    CR_CUDA(ctx, cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, (cudaStream_t)stream),
             "cloud read");
     return CR_OK;
 }
@@ -508,10 +511,64 @@ int64_t cr_cloud_num_batches(const cr_cloud* c) { return c ? c->nb : -1; }
 
 cr_status cr_cloud_destroy(cr_ctx* ctx, cr_cloud* c) {
     if (!c) return CR_ERR_INVALID_ARG;
-    void* ptrs[6] = {c->batches, c->lo, c->md, c->hi, c->rgba, c->verts};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+    if (c->owned) {
+        void* ptrs[6] = {c->batches, c->lo, c->md, c->hi, c->rgba, c->verts};
+        for (void* p : ptrs)
+            if (p) cudaFree(p);
+    }
     delete c;
+    return CR_OK;
+}
+
+namespace {
+
+// True when kernels on `device` may dereference p: device memory or pinned host
+// memory mapped under unified addressing (the device pointer equals p), or any
+// other host memory when the device reads pageable memory directly.
+bool device_addressable(const void* p, int device) {
+    cudaPointerAttributes a;
+    std::memset(&a, 0, sizeof(a));
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return a.devicePointer == p && (a.type == cudaMemoryTypeManaged || a.device == device);
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+    int pageable = 0;
+    return cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess &&
+           pageable == 1;
+}
+
+}  // namespace
+
+cr_status cr_cloud_wrap(cr_ctx* ctx, int64_t n, int64_t nb, int32_t nfiles, const cr_batch* batches,
+                        const uint32_t* lo, const uint32_t* md, const uint32_t* hi,
+                        const uint32_t* rgba, int64_t stream_words, cr_cloud** out) {
+    if (!ctx || !out || !batches || !lo || n < 0 || nb < 0 || n >= ((int64_t)1 << 31) ||
+        nfiles < 1 || nfiles > kInlineFiles || stream_words < n + kStreamPad)
+        return fail(ctx, CR_ERR_INVALID_ARG, "bad wrapped cloud arguments%s", "");
+    *out = nullptr;
+    const void* arrays[5] = {batches, lo, md, hi, rgba};
+    const char* names[5] = {"batches", "xyz_low", "xyz_med", "xyz_hig", "rgba"};
+    for (int i = 0; i < 5; i++)
+        if (arrays[i] && !device_addressable(arrays[i], ctx->device))
+            return fail(ctx, CR_ERR_INVALID_ARG, "%s is not memory the GPU can address", names[i]);
+    cr_cloud* c = new (std::nothrow) cr_cloud();
+    if (!c) return CR_ERR_OUT_OF_MEMORY;
+    c->owned = false;
+    c->n = n;
+    c->nb = nb;
+    c->nfiles = nfiles;
+    c->capacity = stream_words;
+    c->batches = const_cast<cr_batch*>(batches);
+    c->lo = const_cast<uint32_t*>(lo);
+    c->md = const_cast<uint32_t*>(md);
+    c->hi = const_cast<uint32_t*>(hi);
+    c->rgba = const_cast<uint32_t*>(rgba);
+    c->mask = CR_STREAM_LOW | (md ? CR_STREAM_MED : 0) | (hi ? CR_STREAM_HIG : 0) | (rgba ? CR_STREAM_RGBA : 0);
+    c->box_min.assign(3 * (size_t)nfiles, 0.0);
+    *out = c;
     return CR_OK;
 }
 

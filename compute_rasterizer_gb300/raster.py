@@ -88,6 +88,27 @@ class Context:
         c.upload(batches, low, med, hig, rgba, box_min, stream)
         return c
 
+    def cloud_wrap(self, num_points: int, num_batches: int, batches, low, med=None, hig=None,
+                   rgba=None, box_min=None, stream_words: int | None = None,
+                   num_files: int = 1) -> "Cloud":
+        """A cloud over caller-owned arrays (cr_cloud_wrap): numpy arrays, or
+        objects with data_ptr() (device or pinned host tensors), each stream
+        holding stream_words >= num_points + 64 words with zeros past the
+        points.  The arrays are referenced, not copied, for the cloud's life."""
+        arrays = [batches, low, med, hig, rgba]
+        addr = [None if a is None else (a.data_ptr() if hasattr(a, "data_ptr") else ptr(a))
+                for a in arrays]
+        words = stream_words if stream_words is not None else int(num_points) + 64
+        h = C.c_void_p()
+        self.check(self.lib.cr_cloud_wrap(self.handle, int(num_points), int(num_batches),
+                                          int(num_files), *addr, int(words), C.byref(h)),
+                   "cloud wrap")
+        c = Cloud(self, h, num_points, num_batches, num_files)
+        c._arrays = arrays
+        if box_min is not None:
+            c.set_files(box_min)
+        return c
+
     def plain_cloud(self, vertices, stream=None) -> "Cloud":
         v = np.ascontiguousarray(vertices, dtype=L.VERTEX_DTYPE)
         h = C.c_void_p()

@@ -164,6 +164,25 @@ int64_t cr_cloud_num_points(const cr_cloud* cloud);
 int64_t cr_cloud_num_batches(const cr_cloud* cloud);
 cr_status cr_cloud_destroy(cr_ctx* ctx, cr_cloud* cloud);
 
+/* A cloud over caller-owned arrays of the layout above, for clouds kept in
+ * host memory.  The reference's loader uploads every stream of every file into
+ * GPU buffers (LasLoaderSparse.cpp:653-713); here, where kernels can read host
+ * memory (pinned memory under unified addressing, or any memory where the
+ * device reports pageable-memory access, as over NVLink-C2C on Grace), a
+ * frame reads only the words its visible batches need across the link, and a
+ * cloud is no longer bounded by device memory.  Each array may be device
+ * memory or such host memory: the library checks that the GPU can address
+ * every one (CR_ERR_INVALID_ARG if not) and never copies, writes or frees
+ * them; the caller keeps them alive and unchanged while frames read them.
+ * Streams hold stream_words >= num_points + 64 words, the words past
+ * num_points zero.  xyz_med, xyz_hig and rgba may be NULL where no method
+ * needs them.  cr_cloud_upload is refused for such a cloud; set each file's
+ * boxMin with cr_cloud_set_files; cr_cloud_destroy releases only the handle. */
+cr_status cr_cloud_wrap(cr_ctx* ctx, int64_t num_points, int64_t num_batches, int32_t num_files,
+                        const cr_batch* batches, const uint32_t* xyz_low, const uint32_t* xyz_med,
+                        const uint32_t* xyz_hig, const uint32_t* rgba, int64_t stream_words,
+                        cr_cloud** out);
+
 /* Plain 16 B/point clouds (LasLoaderStandard.h). */
 cr_status cr_cloud_create_plain(cr_ctx* ctx, int64_t num_points, cr_cloud** out);
 cr_status cr_cloud_upload_plain(cr_ctx* ctx, cr_cloud* cloud, const cr_vertex* vertices,

@@ -2,9 +2,9 @@
 the oracle, bit for bit, on the full workloads -- the 1B-point terrain at
 1920x1080 (loop_las with both payloads, loop_las_prefetch, HQS), the
 100M-point terrain from all five flight poses at 2560x1440 and with HQS, and
-every view of the 64-view multi-view frame against its single-view render.  The clouds are generated on the GPU (the
-generator is bit-identical to the host one) and read back for the oracle,
-which runs on all host cores."""
+every view of the 64-view multi-view frame against its single-view render.
+The clouds are generated on the GPU (the generator is bit-identical to the
+host one) and read back for the oracle, which runs on all host cores."""
 import os
 
 import numpy as np

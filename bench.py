@@ -570,9 +570,11 @@ def serving(ctx, sh, args, payload):
         return [Server.request(c, cr.make_view(v, p, w, h), host_slot(w * h), user_tag=i)
                 for i, (c, v, p, w, h) in enumerate(cams)]
 
+    # each arm at its best measured setting on this workload: batched launches
+    # of up to 16 views, 4 in flight; plain launches, 8 in flight
     def server(plain):
-        srv = Server(ctx, pool_bytes=8 << 30, max_batch_views=64, max_inflight=2,
-                     plain_launches=plain, payload=payload)
+        srv = Server(ctx, pool_bytes=8 << 30, max_batch_views=1 if plain else 16,
+                     max_inflight=8 if plain else 4, plain_launches=plain, payload=payload)
         for c in clouds:
             srv.add_cloud(c)
         return srv
@@ -580,7 +582,8 @@ def serving(ctx, sh, args, payload):
     arms = {"batched": server(False), "plain": server(True)}
     out = {"clouds_mpoints": list(workloads.SERVING_CLOUD_MPOINTS),
            "resolutions": [f"{w}x{h}" for w, h in workloads.SERVING_RESOLUTIONS],
-           "zipf_s": 1.1, "pool_bytes": 8 << 30, "max_batch_views": 64, "max_inflight": 2,
+           "zipf_s": 1.1, "pool_bytes": 8 << 30, "max_batch_views": 16,
+           "max_inflight": {"batched": 4, "plain": 8},
            "payload": "color" if payload == L.PAYLOAD_COLOR else "index",
            "latency": "arrival -> image in pinned host memory (server clock)"}
     # warm-up

@@ -25,8 +25,8 @@ def request_bytes(width: int, height: int) -> int:
 
 
 class Server:
-    def __init__(self, ctx, *, pool_bytes: int = 8 << 30, max_batch_views: int = 64,
-                 max_inflight: int = 2, max_queued: int = 65536, plain_launches: bool = False,
+    def __init__(self, ctx, *, pool_bytes: int = 8 << 30, max_batch_views: int = 16,
+                 max_inflight: int = 4, max_queued: int = 65536, plain_launches: bool = False,
                  method: int = L.METHOD_LOOP_LAS, payload: int = L.PAYLOAD_COLOR,
                  quirks: int = L.QUIRKS_METHOD_DEFAULT, frustum_culling: bool = True,
                  views_per_group: int = 8, block_threads: int = 0):

@@ -45,8 +45,8 @@ typedef struct cr_server cr_server;
 
 typedef struct cr_server_config {
     int64_t pool_bytes;       /* framebuffer + image pool; 0 = 8 GiB; <= CR_SERVE_MAX_POOL_BYTES */
-    int32_t max_batch_views;  /* views per multi-view launch; 0 = 64 */
-    int32_t max_inflight;     /* launch slots (streams) in flight; 0 = 2 */
+    int32_t max_batch_views;  /* views per multi-view launch; 0 = 16 */
+    int32_t max_inflight;     /* launch slots (streams) in flight; 0 = 4 */
     int32_t max_queued;       /* queued requests before submit refuses; 0 = 65536 */
     int32_t plain_launches;   /* 1: one single-view render per request */
     int32_t method;           /* CR_METHOD_LOOP_LAS or CR_METHOD_LOOP_LAS_PREFETCH */

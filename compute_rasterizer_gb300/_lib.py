@@ -149,6 +149,7 @@ _SIGS = {
     "cr_cloud_set_files": (I32, [P, P, P]),
     "cr_cloud_read": (I32, [P, P, I32, P, I64, P]),
     "cr_cloud_num_points": (I64, [P]),
+    "cr_cloud_set_loaded": (I32, [P, P, I64, I64]),
     "cr_cloud_num_batches": (I64, [P]),
     "cr_cloud_destroy": (I32, [P, P]),
     "cr_cloud_wrap": (I32, [P, I64, I64, I32, P, P, P, P, P, I64, PP]),

@@ -48,7 +48,14 @@ struct cr_cloud {
     cr_vertex* verts = nullptr;
     std::vector<double> box_min;
     bool owned = true;  // false: arrays belong to the caller (cr_cloud_wrap)
+    // points and batch records loaded so far (cr_cloud_set_loaded); -1 = all
+    int64_t n_loaded = -1, nb_loaded = -1;
 };
+
+namespace {
+int64_t loaded_points(const cr_cloud* c) { return c->n_loaded < 0 ? c->n : c->n_loaded; }
+int64_t loaded_batches(const cr_cloud* c) { return c->nb_loaded < 0 ? c->nb : c->nb_loaded; }
+}  // namespace
 
 struct cr_fb {
     int32_t W = 0, H = 0, kind = 0;
@@ -238,8 +245,10 @@ bool cr::cloud_info(const cr_cloud* c, CloudInfo* out) {
     out->md = c->md;
     out->hi = c->hi;
     out->rgba = c->rgba;
-    out->n = c->n;
-    out->nb = c->nb;
+    out->n = loaded_points(c);
+    out->nb = loaded_batches(c);
+    out->n_total = c->n;
+    out->nb_total = c->nb;
     out->capacity = c->capacity;
     out->nfiles = c->nfiles;
     out->box_min = c->box_min.data();
@@ -507,6 +516,19 @@ cr_status cr_cloud_read(cr_ctx* ctx, const cr_cloud* c, int32_t which, void* dst
 }
 
 int64_t cr_cloud_num_points(const cr_cloud* c) { return c ? c->n : -1; }
+
+cr_status cr_cloud_set_loaded(cr_ctx* ctx, cr_cloud* c, int64_t points, int64_t batches) {
+    if (!c) return CR_ERR_INVALID_ARG;
+    if (points < 0 && batches < 0) {
+        c->n_loaded = c->nb_loaded = -1;
+        return CR_OK;
+    }
+    if (points < 0 || points > c->n || (!c->plain && (batches < 0 || batches > c->nb)))
+        return fail(ctx, CR_ERR_INVALID_ARG, "loaded counts exceed the cloud%s", "");
+    c->n_loaded = points;
+    c->nb_loaded = c->plain ? -1 : batches;
+    return CR_OK;
+}
 int64_t cr_cloud_num_batches(const cr_cloud* c) { return c ? c->nb : -1; }
 
 cr_status cr_cloud_destroy(cr_ctx* ctx, cr_cloud* c) {
@@ -766,7 +788,8 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
         mark(1, -1);
         const int grid = ctx->num_sms * 8;
         const int variant = p->method == CR_METHOD_DEDUP ? 1 : (p->method == CR_METHOD_EARLYZ_REDUCE ? 2 : 0);
-        if (launch_plain(T, fb->W, fb->H, cloud->verts, cloud->n, fb->fb, grid, variant, stream) != 0)
+        if (launch_plain(T, fb->W, fb->H, cloud->verts, loaded_points(cloud), fb->fb, grid, variant,
+                         stream) != 0)
             return fail(ctx, CR_ERR_CUDA, "plain raster launch failed%s", "");
         mark(2, CR_STAGE_RASTER);
         mark(3, -1);
@@ -782,9 +805,11 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     s = build_view_params(ctx, cloud, view, p->frustum_culling, &vp);
     vp.lod_skip_level = p->lod_skip_level;
     if (s != CR_OK) return s;
-    int64_t nb = cloud->nb;
+    // the loader's numBatchesLoaded / numPointsLoaded (compute_loop_las.h:233,
+    // compute_loop_las2.h:234)
+    int64_t nb = loaded_batches(cloud);
     if (quirks & CR_QUIRK_DISPATCH_BY_POINTS)
-        nb = std::min<int64_t>(nb, (cloud->n + kPointsPerBatch - 1) / kPointsPerBatch);
+        nb = std::min<int64_t>(nb, (loaded_points(cloud) + kPointsPerBatch - 1) / kPointsPerBatch);
     s = ensure_scratch(ctx, nb);
     if (s != CR_OK) return s;
     ctx->last_dispatched = nb;

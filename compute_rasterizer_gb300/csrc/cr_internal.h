@@ -120,7 +120,9 @@ struct CloudInfo {
     const uint32_t* md;
     const uint32_t* hi;
     const uint32_t* rgba;
-    int64_t n, nb, capacity;
+    int64_t n, nb;              // points and batch records loaded (what frames dispatch)
+    int64_t n_total, nb_total;  // allocated points and batch records
+    int64_t capacity;
     int32_t nfiles;
     const double* box_min;  // 3 * nfiles
 };

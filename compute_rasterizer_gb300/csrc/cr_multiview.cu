@@ -497,7 +497,9 @@ using namespace cr;
 
 struct cr_mv {
     cr_ctx* ctx = nullptr;
-    CloudInfo ci{};
+    const cr_cloud* cloud = nullptr;
+    CloudInfo ci{};            // refreshed every frame (the loaded counts may grow)
+    int64_t graph_n = -1, graph_nb = -1;  // loaded counts the captured graph dispatches
     int32_t nviews = 0;
     std::vector<int32_t> W, H;
     std::vector<int64_t> fb_off, img_off;
@@ -609,6 +611,7 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
     cr_mv* mv = new (std::nothrow) cr_mv();
     if (!mv) return CR_ERR_OUT_OF_MEMORY;
     mv->ctx = ctx;
+    mv->cloud = cloud;
     if (!cloud_info(cloud, &mv->ci) || !mv->ci.md || !mv->ci.hi || mv->ci.nfiles > kInlineFiles) {
         delete mv;
         return CR_ERR_INVALID_ARG;
@@ -646,8 +649,8 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
     if (e == cudaSuccess) e = cudaMalloc(&mv->images, std::max<int64_t>(pixels, 1) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&mv->d_views, sizeof(MVView) * nviews);
     if (e == cudaSuccess) e = cudaMalloc(&mv->d_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles);
-    if (e == cudaSuccess) e = cudaMalloc(&mv->scratch, mv_scratch_words(mv->ci.nb, nviews) * 4);
-    if (e == cudaSuccess) e = cudaMemset(mv->scratch, 0, mv_scratch_words(mv->ci.nb, nviews) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&mv->scratch, mv_scratch_words(mv->ci.nb_total, nviews) * 4);
+    if (e == cudaSuccess) e = cudaMemset(mv->scratch, 0, mv_scratch_words(mv->ci.nb_total, nviews) * 4);
     if (e == cudaSuccess) e = cudaHostAlloc(&mv->h_views, sizeof(MVView) * nviews, cudaHostAllocDefault);
     if (e == cudaSuccess)
         e = cudaHostAlloc(&mv->h_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles, cudaHostAllocDefault);
@@ -718,6 +721,10 @@ cr_status cr_mv_render(cr_mv* mv, int32_t use_graph, void* stream) {
     if (!mv) return CR_ERR_INVALID_ARG;
     const NvtxRange range("cr_mv_render");
     if (!mv->views_set) return mv_fail(mv, CR_ERR_INVALID_ARG, "cr_mv_set_views first");
+    // the cloud's loaded counts may have grown since the last frame; a graph
+    // captured for other counts is dropped and captured again
+    if (!cloud_info(mv->cloud, &mv->ci)) return mv_fail(mv, CR_ERR_INVALID_ARG, "cloud");
+    if (mv->exec && (mv->graph_n != mv->ci.n || mv->graph_nb != mv->ci.nb)) drop_graph(mv);
     cudaStream_t st = (cudaStream_t)stream;
     cr_status s = CR_OK;
     if (use_graph && st != nullptr) {
@@ -733,6 +740,8 @@ cr_status cr_mv_render(cr_mv* mv, int32_t use_graph, void* stream) {
             }
             if (e != cudaSuccess) return mv_cuda(mv, e, "end capture");
             mv->graph = g;
+            mv->graph_n = mv->ci.n;
+            mv->graph_nb = mv->ci.nb;
             e = cudaGraphInstantiate(&mv->exec, g, 0);
             if (e != cudaSuccess) {
                 drop_graph(mv);

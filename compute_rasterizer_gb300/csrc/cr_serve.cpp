@@ -122,7 +122,8 @@ struct cr_server {
     std::chrono::steady_clock::time_point t0;
 
     std::mutex cloud_mu;
-    std::vector<CloudInfo> clouds;
+    std::vector<CloudInfo> clouds;        // as registered (layout, files)
+    std::vector<const cr_cloud*> handles;  // re-read per launch: loaded counts may grow
 
     uint64_t* pool = nullptr;
     PoolAlloc alloc;  // dispatcher thread only
@@ -387,6 +388,7 @@ bool launch(cr_server* s, Slot& sl, std::deque<Pending>& queue) {
     {
         std::lock_guard<std::mutex> lk(s->cloud_mu);
         ci = s->clouds[cloud];
+        cr::cloud_info(s->handles[cloud], &ci);
     }
     const char* what = "";
     sl.t_launch = now_us(s);
@@ -578,6 +580,7 @@ cr_status cr_server_add_cloud(cr_server* s, const cr_cloud* cloud, int32_t* id) 
     std::lock_guard<std::mutex> lk(s->cloud_mu);
     *id = (int32_t)s->clouds.size();
     s->clouds.push_back(ci);
+    s->handles.push_back(cloud);
     return CR_OK;
 }
 

@@ -179,6 +179,12 @@ class Cloud:
             "cloud upload")
         self.ctx.sync(stream)
 
+    def set_loaded(self, points: int = -1, batches: int = -1):
+        """Frames draw only the first `batches` records / `points` points (the
+        loader's numBatchesLoaded / numPointsLoaded); -1, -1 = everything."""
+        self.ctx.check(self.ctx.lib.cr_cloud_set_loaded(self.ctx.handle, self.handle, int(points),
+                                                        int(batches)), "set loaded")
+
     def set_files(self, box_min):
         bm = np.ascontiguousarray(box_min, dtype=np.float64).reshape(-1)
         self.ctx.check(self.ctx.lib.cr_cloud_set_files(self.ctx.handle, self.handle, ptr(bm)),

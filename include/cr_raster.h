@@ -161,6 +161,14 @@ cr_status cr_cloud_set_files(cr_ctx* ctx, cr_cloud* cloud, const double* file_bo
 cr_status cr_cloud_read(cr_ctx* ctx, const cr_cloud* cloud, int32_t which, void* host_dst,
                         int64_t bytes, void* stream);
 int64_t cr_cloud_num_points(const cr_cloud* cloud);
+/* The loader's numPointsLoaded / numBatchesLoaded (LasLoaderSparse.h:77-91):
+ * frames dispatch only the first `batches` records (or, for the methods that
+ * dispatch by points, ceil(points / 10240) of them: compute_loop_las2.h:234),
+ * so a cloud can be drawn while its load tasks are still arriving.  Records
+ * past `batches` are not read.  points <= the cloud's points, batches <= its
+ * records (a plain cloud ignores batches); both negative: everything, the
+ * default. */
+cr_status cr_cloud_set_loaded(cr_ctx* ctx, cr_cloud* cloud, int64_t points, int64_t batches);
 int64_t cr_cloud_num_batches(const cr_cloud* cloud);
 cr_status cr_cloud_destroy(cr_ctx* ctx, cr_cloud* cloud);
 

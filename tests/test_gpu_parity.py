@@ -385,3 +385,58 @@ def test_plain_warp_variants(ctx, method, variant, n, w, h):
     assert np.array_equal(fb.read(L.FB_WORDS)[:w * h], recleared[:w * h])
     fb.close()
     cloud.close()
+
+
+@pytest.mark.parametrize("loaded", [(2 * 10240 + 5, 4), (0, 0)])
+@pytest.mark.parametrize("method", [L.METHOD_LOOP_LAS, L.METHOD_LOOP_LAS_PREFETCH,
+                                    L.METHOD_LOOP_LAS_HQS])
+def test_partially_loaded_cloud(ctx, small, method, loaded):
+    """numPointsLoaded / numBatchesLoaded: with 4 records and 20,485 points
+    loaded, loop_las dispatches 4 records and the methods that dispatch by
+    points ceil(20485 / 10240) = 3; the oracle gets the same prefix."""
+    cl, cloud = small
+    points, batches = loaded
+    cloud.set_loaded(points, batches)
+    try:
+        cam = cameras(cl)["far"]
+        fb, params = gpu_raw(ctx, cloud, cam, method, L.PAYLOAD_INDEX)
+        fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[method])
+        args = (cl["batches"][:batches], points, cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+        if method == L.METHOD_LOOP_LAS_HQS:
+            depth, accum, _ = O.hqs(fr, *args)
+            assert np.array_equal(fb.read(L.FB_DEPTH), depth)
+            assert np.array_equal(fb.read(L.FB_ACCUM), accum)
+        else:
+            want = O.raster_batched(fr, *args)
+            got = fb.read(L.FB_WORDS)
+            assert np.array_equal(got, want), first_diff(got, want)
+            if points == 0:
+                assert (got == L.DEFAULT_CLEAR).all()
+        fb.close()
+    finally:
+        cloud.set_loaded(-1, -1)
+
+
+def test_loaded_counts_reach_multiview_plans(ctx, small):
+    """A plan (CUDA graph replay included) draws what is loaded at each frame."""
+    import torch
+    from compute_rasterizer_gb300.multiview import MultiView
+    cl, cloud = small
+    cams = [cameras(cl)[k] for k in ("far", "mid")]
+    params = default_params(L.METHOD_LOOP_LAS, resolve=0, clear_after=0)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    st = torch.cuda.Stream()
+    try:
+        for points, batches in ((-1, -1), (3 * 10240, 3), (-1, -1)):
+            cloud.set_loaded(points, batches)
+            mv.clear(stream=st.cuda_stream)
+            mv.render(True, st.cuda_stream)
+            ctx.sync(st.cuda_stream)
+            for i, cam in enumerate(cams):
+                fb, _ = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS)
+                assert np.array_equal(mv.read(i, L.FB_WORDS), fb.read(L.FB_WORDS)), (points, i)
+                fb.close()
+    finally:
+        cloud.set_loaded(-1, -1)
+        mv.close()

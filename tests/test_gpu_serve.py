@@ -227,3 +227,27 @@ def test_injected_launch_failure_does_not_wedge_the_loop(ctx, scenes):
     s = srv.stats()
     assert s["failed"] == len(failed) and s["pool_used_bytes"] == 0
     srv.close()
+
+
+def test_server_draws_the_loaded_part(ctx, scenes):
+    """The server reads a cloud's loaded counts at every launch."""
+    clouds, reqs = scenes
+    srv = Server(ctx, pool_bytes=64 << 20)
+    ids = [srv.add_cloud(c) for c in clouds]
+    c0, cam0 = [r for r in reqs if r[0] == 1][0]
+    cloud = clouds[c0]
+    try:
+        for points, batches in ((5 * 10240, 5), (-1, -1)):
+            cloud.set_loaded(points, batches)
+            img = np.zeros(cam0[2] * cam0[3], np.uint32)
+            srv.submit(Server.request(ids[c0], make_view(*cam0), img))
+            srv.drain(60000)
+            (done,) = srv.poll()
+            assert done.status == L.OK
+            fb, params = gpu_raw(ctx, cloud, cam0, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+            ctx.resolve(cloud, params, fb)
+            assert np.array_equal(img, fb.read(L.FB_IMAGE)), points
+            fb.close()
+    finally:
+        cloud.set_loaded(-1, -1)
+        srv.close()

@@ -604,7 +604,7 @@ def serving(ctx, sh, args, payload):
     out["capacity_mean_batch_views"] = round(cap["batched"]["mean_batch_views"], 2)
 
     rates = ([100, 250, 500, 1000, 2000, 3000, 4000, 5000] if args.serving == "full"
-             else [500, 2000, 5000])
+             else [100, 500, 1000, 2000, 5000])
     seconds = 2.0 if args.serving == "full" else 1.0
     sweep = []
     for k, rate in enumerate(rates):

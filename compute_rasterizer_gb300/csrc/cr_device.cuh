@@ -240,5 +240,101 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
     return project_finish(c, px, py, pw, pix, wbits);
 }
 
+// ---- packed fp32 pairs ------------------------------------------------------
+//
+// fma.rn.f32x2 / mul.rn.f32x2 (sm_100 family) do two IEEE single-precision
+// operations, each rounded on its own exactly like __fmaf_rn / __fmul_rn, in
+// one instruction.  Two points of a lane go through the decode and the
+// projection side by side, which halves those float instructions on the
+// issue-bound raster without changing a bit of any result.  The uniforms the
+// pairs need, (u, u) for each uniform u, sit in the kernel parameters: with a
+// fixed file index every operand is a constant-bank operand and needs no
+// register.
+struct PairFile {
+    uint64_t T[12];  // (T[k], T[k]) for T0, T1, T3, T4, T5, T7, T8, T9, T11, T12, T13, T15
+};
+struct PairParams {
+    PairFile files[kInlineFiles];
+    uint64_t half, Wf, Hf;  // (0.5, 0.5), (W, W), (H, H)
+};
+
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+// A batch's 10-bit decode uniforms as pairs (per batch, in registers).
+struct PairBatch {
+    uint64_t sx, sy, sz, mnx, mny, mnz;
+};
+__device__ __forceinline__ PairBatch pair_batch(const BatchCtx& c) {
+    return PairBatch{f2_pack(c.sx, c.sx), f2_pack(c.sy, c.sy), f2_pack(c.sz, c.sz),
+                     f2_pack(c.mnx, c.mnx), f2_pack(c.mny, c.mny), f2_pack(c.mnz, c.mnz)};
+}
+
+// Two 10-bit points (words a0, a1) through decode_point<2> and project(), as
+// pairs: the same operations in the same order, element by element.
+__device__ __forceinline__ void project_pair10(const PairFile& f, const PairParams& pp,
+                                               const PairBatch& b, int32_t W, uint32_t a0,
+                                               uint32_t a1, bool ok[2], int32_t pix[2],
+                                               uint32_t wbits[2]) {
+    const uint64_t X = f2_fma(f2_pack(small_u2f(a0 & 1023u), small_u2f(a1 & 1023u)), b.sx, b.mnx);
+    const uint64_t Y =
+        f2_fma(f2_pack(small_u2f((a0 >> 10) & 1023u), small_u2f((a1 >> 10) & 1023u)), b.sy, b.mny);
+    const uint64_t Z =
+        f2_fma(f2_pack(small_u2f((a0 >> 20) & 1023u), small_u2f((a1 >> 20) & 1023u)), b.sz, b.mnz);
+    // project_clip: T0 T1 T3 T4 T5 T7 T8 T9 T11 T12 T13 T15 are T[0..11]
+    const uint64_t PX = f2_fma(f.T[6], Z, f2_fma(f.T[3], Y, f2_fma(f.T[0], X, f.T[9])));
+    const uint64_t PY = f2_fma(f.T[7], Z, f2_fma(f.T[4], Y, f2_fma(f.T[1], X, f.T[10])));
+    const uint64_t PW = f2_fma(f.T[8], Z, f2_fma(f.T[5], Y, f2_fma(f.T[2], X, f.T[11])));
+    float pw[2];
+    f2_unpack(PW, pw[0], pw[1]);
+    // project_finish
+    const uint64_t R = f2_pack(__frcp_rn(pw[0]), __frcp_rn(pw[1]));
+    const uint64_t QX = f2_mul(PX, R), QY = f2_mul(PY, R);
+    const uint64_t FX = f2_mul(f2_fma(QX, pp.half, pp.half), pp.Wf);
+    const uint64_t FY = f2_mul(f2_fma(QY, pp.half, pp.half), pp.Hf);
+    float qx[2], qy[2], fx[2], fy[2];
+    f2_unpack(QX, qx[0], qx[1]);
+    f2_unpack(QY, qy[0], qy[1]);
+    f2_unpack(FX, fx[0], fx[1]);
+    f2_unpack(FY, fy[0], fy[1]);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        ok[k] = pw[k] > 0.0f && qx[k] >= -1.0f && qx[k] <= 1.0f && qy[k] >= -1.0f && qy[k] <= 1.0f;
+        pix[k] = small_f2i(fx[k]) + small_f2i(fy[k]) * W;
+        wbits[k] = __float_as_uint(pw[k]);
+    }
+}
+
+// Host side: the pair uniforms of every file of a view.
+inline void fill_pair_params(const ViewParams& vp, PairParams* pp) {
+    auto dup = [](float f) {
+        uint32_t u;
+        __builtin_memcpy(&u, &f, 4);
+        return ((uint64_t)u << 32) | u;
+    };
+    static const int kIdx[12] = {0, 1, 3, 4, 5, 7, 8, 9, 11, 12, 13, 15};
+    for (int f = 0; f < kInlineFiles; f++)
+        for (int k = 0; k < 12; k++) pp->files[f].T[k] = dup(vp.files[f].T[kIdx[k]]);
+    pp->half = dup(0.5f);
+    pp->Wf = dup((float)vp.W);
+    pp->Hf = dup((float)vp.H);
+}
+
 }  // namespace
 }  // namespace cr

@@ -174,11 +174,14 @@ __device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, c
 // LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0).
 // Points [first, first + count) are read as 128-bit vectors starting at the
 // aligned word below `first`; lanes mask the words outside the range.  The
-// next vector is loaded before the current one is processed.
-template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false>
+// next vector is loaded before the current one is processed.  PF >= 0 (full
+// 10-bit batches of file PF): points are decoded and projected in pairs with
+// the file's uniforms from the kernel parameters (project_pair10).
+template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false, int PF = -1>
 __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned long long* zc,
-                                           const BatchCtx& c, int64_t first, int32_t count,
-                                           bool l0_x12) {
+                                           const BatchCtx& c, const PairParams& pp, int64_t first,
+                                           int32_t count, bool l0_x12) {
+    static_assert(PF < 0 || (FULL && LC == 2), "pairs decode full 10-bit batches");
     constexpr bool kNeedColor = (MODE == kModeHqsColor) || (MODE == kModeRaster && PAYLOAD == CR_PAYLOAD_COLOR);
     const int64_t v0 = first >> 2;
     const int32_t head = (int32_t)(first & 3);
@@ -190,6 +193,8 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
     const uint4* co4 = reinterpret_cast<const uint4*>(bl.rgba) + v0;
     const uint4 zero = make_uint4(0, 0, 0, 0);
     uint4 n4 = zero, n8 = zero, n12 = zero, ncol = zero;
+    PairBatch pb{};
+    if constexpr (PF >= 0) pb = pair_batch(c);
     if ((int)threadIdx.x < nv) {
         n4 = ld_stream(lo4 + threadIdx.x);
         if (LC <= 1) n8 = ld_stream(md4 + threadIdx.x);
@@ -216,12 +221,17 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             int32_t pix[4];
             uint32_t wb[4];
             bool ok[4];
+            if constexpr (PF >= 0) {
+                project_pair10(pp.files[PF], pp, pb, c.W, w4.x, w4.y, ok, pix, wb);
+                project_pair10(pp.files[PF], pp, pb, c.W, w4.z, w4.w, ok + 2, pix + 2, wb + 2);
+            } else {
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
-                float x, y, z;
-                decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
-                ok[j] = project(c, x, y, z, pix[j], wb[j]) && valid;
+                for (int j = 0; j < 4; j++) {
+                    const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
+                    float x, y, z;
+                    decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
+                    ok[j] = project(c, x, y, z, pix[j], wb[j]) && valid;
+                }
             }
             bool cont[4];
             float lim[4];
@@ -250,6 +260,23 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
                 }
             }
             hqs_color_flush(bl, ok[3] && bc != 0u, pix[3], rg, bc);
+        } else if constexpr (PF >= 0) {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                int32_t pix[2];
+                uint32_t wb[2];
+                bool ok[2];
+                project_pair10(pp.files[PF], pp, pb, c.W, h ? w4.z : w4.x, h ? w4.w : w4.y, ok,
+                               pix, wb);
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int j = 2 * h + k;
+                    const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
+                    const uint32_t color = kNeedColor ? u4get(col, j) : 0u;
+                    const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? color : idx;
+                    Emit<MODE>::run(bl, zc, ok[k], pix[k], wb[k], payload, color);
+                }
+            }
         } else {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -268,6 +295,32 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
     }
 }
 
+// Files whose full 10-bit batches take the paired body, one instance per file.
+// The HQS color pass pairs file 0 only: with more instances its register count
+// goes far past the 48 at which 10 CTAs of 128 threads stay resident per SM.
+template <int MODE>
+constexpr int kPairedFiles = MODE == kModeHqsColor ? 1 : kInlineFiles;
+// The HQS color pass's 10-bit instance is held to those 48 registers (its
+// uncapped 51 leave 9 CTAs per SM; measured 1 % slower).
+template <int MODE, int BLOCK, int LIST>
+constexpr int kMinBlocks = MODE == kModeHqsColor && LIST == 0 ? 1280 / BLOCK : 0;
+
+// A full, vector-aligned 10-bit batch of file `fi`: the paired body with the
+// file's uniforms at a fixed parameter offset, or the scalar one.
+template <int MODE, int PAYLOAD, int BLOCK, int F = 0>
+__device__ __forceinline__ void run_full10(int fi, const BatchedLaunch& bl, unsigned long long* zc,
+                                           const BatchCtx& c, const PairParams& pp, int64_t first,
+                                           bool l0_x12) {
+    if constexpr (F < kPairedFiles<MODE>) {
+        if (fi == F)
+            run_points<MODE, PAYLOAD, BLOCK, 2, true, F>(bl, zc, c, pp, first, kPointsPerBatch, l0_x12);
+        else
+            run_full10<MODE, PAYLOAD, BLOCK, F + 1>(fi, bl, zc, c, pp, first, l0_x12);
+    } else {
+        run_points<MODE, PAYLOAD, BLOCK, 2, true>(bl, zc, c, pp, first, kPointsPerBatch, l0_x12);
+    }
+}
+
 // LIST 0: the 10-bit items (front of the list region), LIST 1: the 20/30-bit
 // items (back of the region).  Each list runs in its own instance, so the
 // common 10-bit instance carries no wider decode state (fewer registers).
@@ -275,7 +328,8 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
 // (programmatic dependent launch); every list-0 CTA waits for the list-1 grid
 // before it exits, so work that follows on the stream sees both lists' writes.
 template <int MODE, int PAYLOAD, int BLOCK, int LIST>
-__global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch bl) {
+__global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
+    k_batched(ViewParams vp, BatchedLaunch bl, PairParams pp) {
     if (LIST == 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ uint32_t s_item[2];
     __shared__ unsigned long long s_zc[MODE == kModeHqsColor ? 1 : kZCacheSlots];
@@ -320,10 +374,10 @@ __global__ void __launch_bounds__(BLOCK) k_batched(ViewParams vp, BatchedLaunch 
             const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
             // full, vector-aligned batches (nearly all) skip the per-point range test
             if (LIST == 0 && count == kPointsPerBatch && (first & 3) == 0)
-                run_points<MODE, PAYLOAD, BLOCK, 2, true>(bl, s_zc, c, first, count, l0_x12);
-            else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, first, count, l0_x12);
-            else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, first, count, l0_x12);
-            else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, first, count, l0_x12);
+                run_full10<MODE, PAYLOAD, BLOCK>(rd.y, bl, s_zc, c, pp, first, l0_x12);
+            else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, pp, first, count, l0_x12);
+            else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, pp, first, count, l0_x12);
+            else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, pp, first, count, l0_x12);
             __syncthreads();
             buf ^= 1;
         }
@@ -552,7 +606,9 @@ static void launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int grid1 = std::min(grid, sms * occupancy_list1<MODE, PAYLOAD, BLOCK>());
-    k_batched<MODE, PAYLOAD, BLOCK, 1><<<grid1, BLOCK, 0, s>>>(vp, bl);
+    PairParams pp;
+    fill_pair_params(vp, &pp);
+    k_batched<MODE, PAYLOAD, BLOCK, 1><<<grid1, BLOCK, 0, s>>>(vp, bl, pp);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(BLOCK);
@@ -563,7 +619,7 @@ static void launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0>, vp, bl);
+    cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0>, vp, bl, pp);
 }
 
 template <int MODE, int PAYLOAD>

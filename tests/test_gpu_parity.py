@@ -218,6 +218,57 @@ def test_unaligned_first_point_multi_file(ctx, pad):
             assert np.array_equal(got, want), (camname, method, first_diff(got, want))
 
 
+@pytest.fixture(scope="module")
+def eight_files(ctx):
+    """Eight files of two full batches each, every file with its own box: full
+    10-bit batches of every file index take the paired decode/projection body
+    with that file's uniforms."""
+    parts, batches, boxes = [], [], []
+    for f in range(8):
+        c = encoded(n=20480, extent=40.0, seed=40 + f)
+        b = c["batches"].copy()
+        b["first_point"] += f * 20480
+        b["file_index"] = f
+        parts.append(c)
+        batches.append(b)
+        boxes.append(c["box_min"] + np.array([50.0 * (f % 4), 50.0 * (f // 4), 3.0 * f]))
+    batches = np.concatenate(batches)
+    streams = [np.concatenate([c[k] for c in parts]) for k in ("lo", "md", "hi", "rgba")]
+    box = np.stack(boxes)
+    tops = np.stack([bx + (c["box_max"] - c["box_min"]) for bx, c in zip(boxes, parts)])
+    cl = dict(n=8 * 20480, batches=batches, box_min=box.min(0), box_max=tops.max(0),
+              streams=streams, boxes=box)
+    return cl, ctx.cloud_from_arrays(batches, *streams, box)
+
+
+@pytest.mark.parametrize("camname", ["far", "corner"])
+@pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
+def test_every_file_index_raster(ctx, eight_files, camname, payload):
+    cl, cloud = eight_files
+    cam = cameras(cl)[camname]
+    fb, _ = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS, payload)
+    fr = oracle_frame(cam, cl["boxes"], QUIRKS[L.METHOD_LOOP_LAS], payload)
+    want = O.raster_batched(fr, cl["batches"], cl["n"], *cl["streams"])
+    got = fb.read(L.FB_WORDS)
+    assert np.array_equal(got, want), first_diff(got, want)
+    if camname == "far" and payload == L.PAYLOAD_INDEX:
+        idx = got[got != L.DEFAULT_CLEAR] & 0xFFFFFFFF
+        assert len(np.unique(idx // 20480)) == 8  # every file wrote pixels
+
+
+@pytest.mark.parametrize("camname", ["far", "corner"])
+def test_every_file_index_hqs(ctx, eight_files, camname):
+    cl, cloud = eight_files
+    cam = cameras(cl)[camname]
+    fb, params = gpu_raw(ctx, cloud, cam, L.METHOD_LOOP_LAS_HQS)
+    fr = oracle_frame(cam, cl["boxes"], QUIRKS[L.METHOD_LOOP_LAS_HQS])
+    depth, accum, img = O.hqs(fr, cl["batches"], cl["n"], *cl["streams"])
+    assert np.array_equal(fb.read(L.FB_DEPTH), depth)
+    assert np.array_equal(fb.read(L.FB_ACCUM), accum)
+    ctx.resolve(cloud, params, fb)
+    assert np.array_equal(fb.read(L.FB_IMAGE), img)
+
+
 def test_hqs_one_pixel_receives_a_million_points(ctx):
     nb = 98
     n = nb * 10240

@@ -142,6 +142,7 @@ _SIGS = {
     "cr_ctx_destroy": (I32, [P]),
     "cr_last_error": (C.c_char_p, [P]),
     "cr_ctx_check": (I32, [P, P]),
+    "cr_check_reciprocal": (I32, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
     "cr_ctx_num_sms": (I32, [P]),
     "cr_cloud_create": (I32, [P, I64, I64, I32, I32, PP]),
     "cr_cloud_upload": (I32, [P, P, P, P, P, P, P, P, P]),

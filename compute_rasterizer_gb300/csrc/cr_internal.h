@@ -107,6 +107,9 @@ int launch_resolve_hqs(int32_t W, int32_t H, uint32_t* depth, uint64_t* accum, u
                        int clear_after, void* stream);
 int launch_fill_u64(uint64_t* p, int64_t n, uint64_t v, void* stream);
 int launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, void* stream);
+// rcp_rn against __frcp_rn over every float; counts into bad[0], the lowest
+// mismatching bit pattern into *first (synchronous, default stream).
+int launch_check_reciprocal(uint64_t* bad, uint32_t* first);
 int batched_blocks_per_sm(int mode, int payload, int block);
 
 // Per-view uniforms from double matrices and per-file boxMin (cr_api.cpp).

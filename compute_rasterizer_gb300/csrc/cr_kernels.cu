@@ -3,8 +3,9 @@
 // Compiled with -fmad=false: every fused multiply-add below is an explicit
 // __fmaf_rn, every other float operation rounds on its own, scalar / and sqrt
 // are IEEE (__fdiv_rn, __fsqrt_rn), and a vector divided by a scalar is a
-// multiplication by the scalar's correctly rounded reciprocal (__frcp_rn), the
-// one reciprocal a shader compiler emits for it.  The operation order follows
+// multiplication by the scalar's correctly rounded reciprocal (rcp_rn, equal
+// to __frcp_rn for every input), the one reciprocal a shader compiler emits
+// for it.  The operation order follows
 // the arithmetic contract the oracle states, which is what makes the
 // framebuffers bit-exact.
 //
@@ -571,6 +572,22 @@ __global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
         p[i] = v;
 }
 
+// Every float bit pattern: rcp_rn(x) against __frcp_rn(x), bit for bit (a NaN
+// matches any NaN).
+__global__ void __launch_bounds__(256) k_check_reciprocal(unsigned long long* bad, uint32_t* first) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long mine = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (1ull << 32); i += stride) {
+        const float x = __uint_as_float((uint32_t)i);
+        const float a = rcp_rn(x), b = __frcp_rn(x);
+        if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) {
+            mine++;
+            atomicMin(first, (uint32_t)i);
+        }
+    }
+    if (mine) atomicAdd(bad, mine);
+}
+
 inline int blocks_for(int64_t n, int per) { return (int)((n + per - 1) / per); }
 
 int launch_status() { return cudaGetLastError() == cudaSuccess ? 0 : -1; }
@@ -717,6 +734,15 @@ int launch_resolve_hqs(int32_t W, int32_t H, uint32_t* depth, uint64_t* accum, u
     k_resolve_hqs<<<blocks_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(P, tail, depth, accum,
                                                                                image, clear_after);
     return launch_status();
+}
+
+int launch_check_reciprocal(uint64_t* bad, uint32_t* first) {
+    int device = 0, sms = 1;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    k_check_reciprocal<<<sms * 8, 256>>>(reinterpret_cast<unsigned long long*>(bad), first);
+    if (launch_status() != 0) return -1;
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -1;
 }
 
 int launch_fill_u64(uint64_t* p, int64_t n, uint64_t v, void* stream) {

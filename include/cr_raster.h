@@ -135,6 +135,11 @@ const char* cr_last_error(const cr_ctx* ctx);
 /* Waits for `stream`, then reports a device-side error flag raised since the
  * last check (CR_ERR_DEVICE_FLAG) and clears it. */
 cr_status cr_ctx_check(cr_ctx* ctx, void* stream);
+/* Self-check of the kernels' reciprocal (the correctly rounded 1/w that every
+ * `xy / w` uses, render.cs:402): runs it against CUDA's __frcp_rn over all 2^32
+ * float bit patterns on the context's device and reports the mismatches (NaN
+ * matches NaN) and the lowest mismatching pattern (0xFFFFFFFF if none). */
+cr_status cr_check_reciprocal(cr_ctx* ctx, uint64_t* mismatches, uint32_t* first_mismatch);
 int32_t cr_ctx_num_sms(const cr_ctx* ctx);
 
 /* ---- clouds: the LAS-derived layout (LasLoaderSparse.h:86-91) ------------ */

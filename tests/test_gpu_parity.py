@@ -152,6 +152,18 @@ def test_golden_digests(ctx):
             assert G.dg(fb.read(L.FB_IMAGE)) == dg["image"], case["name"]
 
 
+def test_reciprocal_matches_frcp_rn_on_every_float(ctx):
+    """The kernels' 1/w (hardware approximation + one Newton step, __frcp_rn
+    outside [2^-126, 2^126)) equals CUDA's correctly rounded __frcp_rn for all
+    2^32 bit patterns, so `xy / w` (render.cs:402) keeps the oracle's
+    correctly rounded reciprocal."""
+    import ctypes as C
+    bad, first = C.c_uint64(), C.c_uint32()
+    ctx.check(ctx.lib.cr_check_reciprocal(ctx.handle, C.byref(bad), C.byref(first)), "rcp check")
+    assert bad.value == 0, hex(first.value)
+    assert first.value == 0xFFFFFFFF
+
+
 # ---- edge cases -------------------------------------------------------------
 
 def run_handmade(ctx, hm, cam, method, payload=L.PAYLOAD_INDEX, quirks=None):

@@ -292,8 +292,13 @@ def main():
     peak, peak_kind = measured_peaks()
     raster_s = float(np.mean(raster_ms)) / 1e3
     achieved = stats.stream_bytes / raster_s / 1e9
+    # DRAM bytes per launch: the ncu traffic / algorithmic ratio of the color
+    # raster (profiles/raster_terrain_1b_traffic.json) times this launch's
+    # algorithmic bytes (the traffic grows with the bytes streamed)
     prof = ROOT / "profiles" / "raster_terrain_1b_traffic.json"
-    traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch") if prof.exists() else None
+    ratio = json.loads(prof.read_text()).get("traffic_over_algorithmic") if prof.exists() else None
+    traffic = (int(round(ratio * stats.stream_bytes))
+               if ratio and args.payload == "color" else None)
 
     out = {"metric": metric_name(), "value": round(value, 3), "unit": "Gpoints/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -230,6 +230,7 @@ struct PairFile {
 struct PairParams {
     PairFile files[kInlineFiles];
     uint64_t half, Wf, Hf;  // (0.5, 0.5), (W, W), (H, H)
+    uint64_t bias;          // (-2^23, -2^23)
 };
 
 __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
@@ -247,17 +248,30 @@ __device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
     asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
     return d;
 }
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 __device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
 }
 
-// A batch's 10-bit decode uniforms as pairs (per batch, in registers).
+// A batch's 10-bit decode uniforms as pairs (per batch, in registers): the
+// steps sx, sy * 2^-10, sz * 2^-20 and the minimum corner (see project_pair10).
 struct PairBatch {
     uint64_t sx, sy, sz, mnx, mny, mnz;
 };
 __device__ __forceinline__ PairBatch pair_batch(const BatchCtx& c) {
-    return PairBatch{f2_pack(c.sx, c.sx), f2_pack(c.sy, c.sy), f2_pack(c.sz, c.sz),
+    const float sy = fmul(c.sy, 0x1p-10f), sz = fmul(c.sz, 0x1p-20f);
+    return PairBatch{f2_pack(c.sx, c.sx), f2_pack(sy, sy), f2_pack(sz, sz),
                      f2_pack(c.mnx, c.mnx), f2_pack(c.mny, c.mny), f2_pack(c.mnz, c.mnz)};
+}
+// Whether sy * 2^-10 and sz * 2^-20 are exact (no underflow: steps of at least
+// 2^-106, or zero, or infinite); batches where they are not take the scalar body.
+__device__ __forceinline__ bool pair_batch_exact(const BatchCtx& c) {
+    return fmul(fmul(c.sy, 0x1p-10f), 0x1p10f) == c.sy &&
+           fmul(fmul(c.sz, 0x1p-20f), 0x1p20f) == c.sz;
 }
 
 // project_finish() for two points: clip positions (PX, PY, PW) as pairs, the
@@ -286,16 +300,27 @@ __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, ui
 }
 
 // Two 10-bit points (words a0, a1) through decode_point<2> and project(), as
-// pairs: the same operations in the same order, element by element.
+// pairs: the same operations in the same order, element by element.  The
+// integer fields reach the decode FMA as floats without shifts: x as the
+// float 2^23 + x (x in the mantissa's low bits) minus 2^23, y as 2^23 + y*2^10
+// minus 2^23, z as float(word & 0x3FF00000) = z*2^20, every value exact.  y
+// and z then meet the steps sy*2^-10 and sz*2^-20, whose products with them
+// are the same real numbers y*sy and z*sz, so each FMA rounds exactly as
+// fma(float(y), sy, min_y) does (measured 1.6 % faster on the color raster,
+// 3.9 % on the index one, than shift, mask and convert per field).
 __device__ __forceinline__ void project_pair10(const PairFile& f, const PairParams& pp,
                                                const PairBatch& b, int32_t W, uint32_t a0,
                                                uint32_t a1, bool ok[2], int32_t pix[2],
                                                uint32_t wbits[2]) {
-    const uint64_t X = f2_fma(f2_pack(small_u2f(a0 & 1023u), small_u2f(a1 & 1023u)), b.sx, b.mnx);
-    const uint64_t Y =
-        f2_fma(f2_pack(small_u2f((a0 >> 10) & 1023u), small_u2f((a1 >> 10) & 1023u)), b.sy, b.mny);
-    const uint64_t Z =
-        f2_fma(f2_pack(small_u2f((a0 >> 20) & 1023u), small_u2f((a1 >> 20) & 1023u)), b.sz, b.mnz);
+    const uint64_t XF = f2_add(f2_pack(__uint_as_float((a0 & 0x3FFu) | 0x4B000000u),
+                                       __uint_as_float((a1 & 0x3FFu) | 0x4B000000u)), pp.bias);
+    const uint64_t YF = f2_add(f2_pack(__uint_as_float((a0 & 0xFFC00u) | 0x4B000000u),
+                                       __uint_as_float((a1 & 0xFFC00u) | 0x4B000000u)), pp.bias);
+    const uint64_t ZF =
+        f2_pack(__uint2float_rn(a0 & 0x3FF00000u), __uint2float_rn(a1 & 0x3FF00000u));
+    const uint64_t X = f2_fma(XF, b.sx, b.mnx);
+    const uint64_t Y = f2_fma(YF, b.sy, b.mny);
+    const uint64_t Z = f2_fma(ZF, b.sz, b.mnz);
     // project_clip: T0 T1 T3 T4 T5 T7 T8 T9 T11 T12 T13 T15 are T[0..11]
     const uint64_t PX = f2_fma(f.T[6], Z, f2_fma(f.T[3], Y, f2_fma(f.T[0], X, f.T[9])));
     const uint64_t PY = f2_fma(f.T[7], Z, f2_fma(f.T[4], Y, f2_fma(f.T[1], X, f.T[10])));
@@ -314,6 +339,7 @@ inline void fill_pair_params(const ViewParams& vp, PairParams* pp) {
     for (int f = 0; f < kInlineFiles; f++)
         for (int k = 0; k < 12; k++) pp->files[f].T[k] = dup(vp.files[f].T[kIdx[k]]);
     pp->half = dup(0.5f);
+    pp->bias = dup(-8388608.0f);
     pp->Wf = dup((float)vp.W);
     pp->Hf = dup((float)vp.H);
 }

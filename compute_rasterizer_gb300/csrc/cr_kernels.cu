@@ -373,8 +373,9 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
             c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
             const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-            // full, vector-aligned batches (nearly all) skip the per-point range test
-            if (LIST == 0 && count == kPointsPerBatch && (first & 3) == 0)
+            // full, vector-aligned batches (nearly all) skip the per-point range
+            // test and decode in pairs; the rest take the general body
+            if (LIST == 0 && count == kPointsPerBatch && (first & 3) == 0 && pair_batch_exact(c))
                 run_full10<MODE, PAYLOAD, BLOCK>(rd.y, bl, s_zc, c, pp, first, l0_x12);
             else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, pp, first, count, l0_x12);

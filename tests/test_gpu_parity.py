@@ -187,6 +187,26 @@ def test_frustum_edge_writes_guard_row(ctx):
     assert (int(got[w * h + w]) & 0xFFFFFFFF) == 7  # last guard entry
 
 
+@pytest.mark.parametrize("axis", [1, 2])
+@pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
+def test_full_batch_with_tiny_extent(ctx, axis, payload):
+    """A full 10-bit batch whose y or z extent is ~1e-33: its step scaled by
+    2^-10 / 2^-20 underflows, so the batch leaves the paired decode for the
+    general body; the framebuffer still matches the oracle."""
+    rng = np.random.default_rng(11 + axis)
+    pts = rng.integers(0, 1024, (10240, 3))
+    colors = rng.integers(0, 1 << 24, 10240)
+    lo, hi = [-1.0, -0.5, 0.0], [1.0, 0.5, 1.0]
+    lo[axis], hi[axis] = 0.0, 1e-33
+    hm = handmade_cloud(pts, colors, box_min=tuple(lo), box_max=tuple(hi))
+    proj = np.eye(4)
+    proj[2, 3], proj[3, 3] = 1.0, 2.0  # column-major: w = z + 2, so z reaches the depth
+    cam = (np.eye(4).reshape(16), proj.reshape(16), 64, 32)
+    got, want = run_handmade(ctx, hm, cam, L.METHOD_LOOP_LAS, payload)
+    assert np.array_equal(got, want), first_diff(got, want)
+    assert (got != L.DEFAULT_CLEAR).sum() > 20
+
+
 @pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
 def test_equal_depth_ties_take_min_payload(ctx, payload):
     pts = [(300, 300, 10)] * 40 + [(301, 300, 10)] * 3

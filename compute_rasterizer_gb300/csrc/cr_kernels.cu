@@ -5,9 +5,10 @@
 // are IEEE (__fdiv_rn, __fsqrt_rn), and a vector divided by a scalar is a
 // multiplication by the scalar's correctly rounded reciprocal (rcp_rn, equal
 // to __frcp_rn for every input), the one reciprocal a shader compiler emits
-// for it.  The operation order follows
-// the arithmetic contract the oracle states, which is what makes the
-// framebuffers bit-exact.
+// for it.  The operation order follows the arithmetic contract the oracle
+// states, which is what makes the framebuffers bit-exact; the packed-pair
+// forms (fma.rn.f32x2, mul.rn.f32x2) round each element as the scalar
+// instructions do.
 //
 // Kernels
 //   k_cull      one thread per batch record: validation, frustum cull
@@ -16,11 +17,13 @@
 //   k_batched   persistent CTAs pull work items; per batch the points are read
 //               with 128-bit streaming loads (4 consecutive points per lane,
 //               the loop_las2 `uvec4` scheme), decoded at 10/20/30 bit,
-//               projected, tested against a per-CTA shared-memory z-cache,
+//               projected (full 10-bit batches two points per packed
+//               instruction), tested against a per-CTA shared-memory z-cache,
 //               and the survivors issue 64-bit atomicMin (render.cs:399-432).
 //               The same body runs the HQS depth pass (u32 atomicMin,
-//               hqs/depth.cs) and color pass (__match_any_sync partitioned
-//               sums + two 64-bit atomicAdd per pixel, hqs/color.cs:388-444).
+//               hqs/depth.cs) and color pass (per-lane run sums; a lane's
+//               last run through __match_any_sync partitioned sums; two
+//               64-bit atomicAdd per pixel, hqs/color.cs:388-444).
 //   k_plain     16 B/point path (compute_2021_earlyz/render.cs:35-74).
 //   k_resolve_* per-pixel resolves (resolve.cs files), optionally re-clearing.
 #include <cuda_runtime.h>

@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--cpu-table", action="store_true",
+                    help="time the oracle per workload on this host's cores and exit")
     ap.add_argument("--serving", default="quick", choices=["quick", "full", "off"])
     ap.add_argument("--extras", default="payloads,multiview,configs,serving",
                     help="comma list of extra workloads after the headline frame")
@@ -209,6 +211,71 @@ def reference_arm(args, world, rank):
     print(json.dumps(out), flush=True)
 
 
+def cpu_table(args):
+    """--cpu-table: the oracle (the reference's CPU restatement) per workload on
+    this host's cores, 1 thread and all threads where the oracle has both, on
+    bounded samples of each workload; one JSON line.  A host-only run."""
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import synth, workloads
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+
+    def rate(fn, points, min_s=3.0):
+        fn()
+        t0, k = time.perf_counter(), 0
+        while k < 1 or time.perf_counter() - t0 < min_s:
+            fn()
+            k += 1
+        return round(points * k / (time.perf_counter() - t0) / 1e9, 4)
+
+    out = {}
+    # plain 16 B path, 4,194,304 points at 1920x1080 (single-threaded oracle)
+    n1, W1, H1 = 4_194_304, 1920, 1080
+    v = synth.uniform_vertices_host(1, n1, 100.0)
+    cam1 = synth.look_at([150.0, 150.0, 150.0], [50.0, 50.0, 50.0], [0.0, 0.0, 1.0])
+    proj1 = synth.perspective(60.0, W1 / H1, 0.1, 1000.0)
+    out["plain_4m_1080p"] = {"threads_1": rate(lambda: O.plain(cam1, proj1, W1, H1, v), n1),
+                             "sample": "the full workload"}
+
+    def batched(points_full, extent, seed, sample, cams, own_bounds=False):
+        p, hdr, enc, ext = cpu_sample(points_full, extent, seed, sample)
+        # streams padded once (the oracle's calls copy unpadded streams every frame)
+        enc = (enc[0], *(O.pad_stream(x, n=sample) for x in enc[1:]))
+        fmin = np.array(hdr.min[:]) if own_bounds else np.array([0.0, 0.0, hdr.min[2]])
+        fmax = np.array(hdr.max[:]) if own_bounds else np.array([extent, extent, hdr.max[2]])
+        r1, rn = [], []
+        for view, proj, w, h in cams(fmin, fmax):
+            fr = O.make_frame(view, proj, w, h, np.array(hdr.min[:])[None], 1, O.L0_X12,
+                              O.PAYLOAD_COLOR)
+            r1.append(rate(lambda: O.raster_batched(fr, enc[0], sample, *enc[1:]), sample, 1.0))
+            rn.append(rate(lambda: O.raster_batched(fr, enc[0], sample, *enc[1:], threads=cores),
+                           sample, 1.0))
+        return r1, rn, ext, enc, hdr, fmin, fmax
+
+    def main_cam(fmin, fmax):
+        view, proj = camera(fmin, fmax, WORKLOAD["width"], WORKLOAD["height"])
+        return [(view, proj, WORKLOAD["width"], WORKLOAD["height"])]
+
+    s2 = 8_000_000
+    r1, rn, ext, _, _, _, _ = batched(100_000_000, 1000.0, 2, s2, workloads.flight_path, True)
+    out["flight_100m_1440p"] = {"threads_1": round(float(np.mean(r1)), 4),
+                                f"threads_{cores}": round(float(np.mean(rn)), 4),
+                                "sample": f"{s2:,} points, the central {ext:.0f} m square at the "
+                                          "same density, the 5 flight poses laid over the sample"}
+    s3 = CPU_SAMPLE_POINTS
+    r1, rn, ext, enc, hdr, fmin, fmax = batched(WORKLOAD["points"], WORKLOAD["extent"],
+                                                WORKLOAD["seed"], s3, main_cam)
+    out["terrain_1b_1080p"] = {"threads_1": r1[0], f"threads_{cores}": rn[0],
+                               "sample": f"{s3:,} points, the central {ext:.0f} m square at the "
+                                         "same density, the same camera"}
+    (view, proj, w, h), = main_cam(fmin, fmax)
+    fr = O.make_frame(view, proj, w, h, np.array(hdr.min[:])[None], 1, O.L0_X12, O.PAYLOAD_INDEX)
+    out["terrain_1b_1080p_hqs"] = {"threads_1": rate(lambda: O.hqs(fr, enc[0], s3, *enc[1:]), s3),
+                                   "sample": out["terrain_1b_1080p"]["sample"]}
+    print(json.dumps({"cpu_table": out, "cores": cores, "unit": "Gpoints/s",
+                      "kind": "port (the oracle)"}), flush=True)
+
+
 def metric_name():
     return "Gpoints/s at 1B points (frame = cull + raster + resolve)"
 
@@ -227,6 +294,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.cpu_table:
+        cpu_table(args)
+        return
     if args.impl == "reference":
         reference_arm(args, world, rank)
         if world > 1:

@@ -533,17 +533,12 @@ __global__ void k_resolve_color(int64_t P, int64_t tail, uint64_t* __restrict__ 
 }
 
 // compute_2021_earlyz/resolve.cs:41-77
+// uvec4(255.0 * unpackUnorm4x8(ucol)) per byte is trunc(255 * RN(c / 255)),
+// which is c again for every byte c (checked over all 256 values, the CPU
+// test test_plain_byte_round_trip), so the image word is ucol itself.
 __device__ __forceinline__ uint32_t plain_rgba8(uint64_t v) {
-    uint32_t ucol = (uint32_t)(v & 0x00FFFFFFull);
-    if (ucol == 0u) return 0xFF000000u;
-    uint32_t o = 0;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        float cf = small_u2f((ucol >> (8 * k)) & 0xFFu);
-        float f = fmul(255.0f, __fdiv_rn(cf, 255.0f));
-        o |= ((uint32_t)small_f2i(f) & 0xFFu) << (8 * k);
-    }
-    return o;
+    const uint32_t ucol = (uint32_t)(v & 0x00FFFFFFull);
+    return ucol == 0u ? 0xFF000000u : ucol;
 }
 
 __global__ void k_resolve_plain(int64_t P, int64_t tail, uint64_t* __restrict__ fb,

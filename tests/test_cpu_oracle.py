@@ -356,3 +356,24 @@ def test_key_packing_orders_by_depth_then_payload():
     pay = rng.integers(0, 2**32, 5000, dtype=np.uint64)
     key = (w.view(np.uint32).astype(np.uint64) << np.uint64(32)) | pay
     assert np.array_equal(np.argsort(key, kind="stable"), np.lexsort((pay, w)))
+
+
+
+def test_plain_byte_round_trip():
+    """compute_2021_earlyz/resolve.cs:41-77 writes uvec4(255.0 * unpackUnorm4x8(ucol)):
+    per byte trunc(255 * RN(c / 255)) in binary32.  That is c again for all 256
+    bytes, so the GPU resolve copies the bytes; the oracle keeps the formula."""
+    c = np.arange(256, dtype=np.float32)
+    back = np.float32(255.0) * (c / np.float32(255.0))
+    assert back.dtype == np.float32
+    assert np.array_equal(np.trunc(back).astype(np.int64), np.arange(256))
+    # the oracle's resolve (the formula) equals the byte copy word for word
+    rng = np.random.default_rng(3)
+    w, h = 64, 32
+    fb = (rng.integers(1, 2**31, w * h + w + 1, dtype=np.uint64) << np.uint64(32)) | \
+        rng.integers(0, 2**32, w * h + w + 1, dtype=np.uint64)
+    fb[::5] &= np.uint64(0xFFFFFFFFFF000000)  # ucol == 0 -> (0, 0, 0, 255)
+    img = np.empty(w * h, dtype=np.uint32)
+    ucol = (fb[: w * h] & np.uint64(0xFFFFFF)).astype(np.uint32)
+    O.lib().or_resolve_plain(w, h, fb.ctypes.data, img.ctypes.data, 0xFFFFFFFFFF3C321E)
+    assert np.array_equal(img, np.where(ucol == 0, np.uint32(0xFF000000), ucol))

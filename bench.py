@@ -276,6 +276,15 @@ def cpu_table(args):
                       "kind": "port (the oracle)"}), flush=True)
 
 
+def max_over_ranks(value: float, device: str = "cuda") -> float:
+    """The slowest rank's value: every rank passes its own, all get the max."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def metric_name():
     return "Gpoints/s at 1B points (frame = cull + raster + resolve)"
 
@@ -348,9 +357,7 @@ def main():
     elapsed = e0.elapsed_time(e1) / 1e3
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+        elapsed = max_over_ranks(elapsed, "cuda")
         dist.barrier()
     ctx.sync(sh)
     raster_ms = ctx.timing_read(L.STAGE_RASTER, args.steps)

@@ -431,7 +431,7 @@ cr_status cr_cloud_create(cr_ctx* ctx, int64_t n, int64_t nb, int32_t nfiles, in
                           cr_cloud** out) {
     if (!ctx || !out) return CR_ERR_INVALID_ARG;
     *out = nullptr;
-    if (n < 0 || nb < 0 || nb >= ((int64_t)1 << 29) || n >= ((int64_t)1 << 31) - kStreamPad ||
+    if (n < 0 || nb < 0 || nb >= kMaxBatches || n >= ((int64_t)1 << 31) - kStreamPad ||
         nfiles < 1 || nfiles > kInlineFiles || (mask & CR_STREAM_LOW) == 0)
         return fail(ctx, CR_ERR_INVALID_ARG, "bad cloud shape %s(n=%lld)", "", (long long)n);
     cr_cloud* c = new (std::nothrow) cr_cloud();
@@ -584,7 +584,8 @@ bool device_addressable(const void* p, int device) {
 cr_status cr_cloud_wrap(cr_ctx* ctx, int64_t n, int64_t nb, int32_t nfiles, const cr_batch* batches,
                         const uint32_t* lo, const uint32_t* md, const uint32_t* hi,
                         const uint32_t* rgba, int64_t stream_words, cr_cloud** out) {
-    if (!ctx || !out || !batches || !lo || n < 0 || nb < 0 || n >= ((int64_t)1 << 31) ||
+    if (!ctx || !out || !batches || !lo || n < 0 || nb < 0 || nb >= kMaxBatches ||
+        n >= ((int64_t)1 << 31) ||
         nfiles < 1 || nfiles > kInlineFiles || stream_words < n + kStreamPad)
         return fail(ctx, CR_ERR_INVALID_ARG, "bad wrapped cloud arguments%s", "");
     *out = nullptr;
@@ -901,7 +902,7 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
     out->batches_dispatched = ctx->last_dispatched;
     out->batches_visible = count;
     for (uint32_t it : items) {
-        const uint32_t b = it & 0x1FFFFFFFu;
+        const uint32_t b = it & kItemBatchMask;
         const int level = (int)(it >> 29);
         if (b >= recs.size() || level > 4) continue;
         int64_t n = recs[b].num_points + ((quirks & CR_QUIRK_INCLUSIVE_END) ? 1 : 0);

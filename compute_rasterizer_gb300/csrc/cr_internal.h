@@ -30,6 +30,13 @@ constexpr uint32_t kHqsDepthClear = 0xFF800000u;           // compute_loop_las_h
 // a partial last batch and the one-past-the-end point of the inclusive bound.
 constexpr int64_t kStreamPad = 64;
 
+// Work items of the single-view lists (k_cull -> k_batched):
+// batch index | kItemWSafe (the clip w of every point of the batch is proven
+// to lie in [2^-120, 2^120]) | precision level << 29.
+constexpr uint32_t kItemBatchMask = 0x0FFFFFFFu;
+constexpr uint32_t kItemWSafe = 1u << 28;
+constexpr int64_t kMaxBatches = (int64_t)1 << 28;
+
 // Device error bits (ctx scratch word kErrWord).
 enum : uint32_t {
     kErrBadBatch = 1u,   // record with num_points/first_point/file_index out of range

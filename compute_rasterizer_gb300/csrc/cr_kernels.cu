@@ -13,7 +13,8 @@
 // Kernels
 //   k_cull      one thread per batch record: validation, frustum cull
 //               (render.cs:176-197), precision level (render.cs:199-231);
-//               appends (batch | level << 29) to a work list.
+//               w-safe flag (w_safe); appends (batch | flag | level << 29)
+//               to a work list.
 //   k_batched   persistent CTAs pull work items; per batch the points are read
 //               with 128-bit streaming loads (4 consecutive points per lane,
 //               the loop_las2 `uvec4` scheme), decoded at 10/20/30 bit,
@@ -64,7 +65,8 @@ __global__ void __launch_bounds__(256) k_cull(ViewParams vp, const cr_batch* __r
                 int level = precision_level(vp.P, f.VW, vp.W, vp.H, mnx, mny, mnz, mxx, mxy, mxz);
                 // compute_loop_nodes/render.cs:273-276: the level-of-detail cut
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
-                item = (uint32_t)b | ((uint32_t)level << 29);
+                item = (uint32_t)b | ((uint32_t)level << 29) |
+                       (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz) ? kItemWSafe : 0u);
             }
         }
     }
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             if (threadIdx.x == 0) s_item[buf ^ 1] = atomicAdd(cursor, 1u);
             const uint32_t item =
                 bl.scratch[kScratchHead + (LIST == 0 ? (int64_t)wi : bl.list_cap - 1 - (int64_t)wi)];
-            const uint32_t b = item & 0x1FFFFFFFu;
+            const uint32_t b = item & kItemBatchMask;
             const int level = (int)(item >> 29);
 
             const int4* r4 = reinterpret_cast<const int4*>(bl.batches + b);
@@ -390,9 +392,11 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
             c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
             const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
-            // full, vector-aligned batches (nearly all) skip the per-point range
-            // test and decode in pairs; the rest take the general body
-            if (LIST == 0 && count == kPointsPerBatch && (first & 3) == 0 && pair_batch_exact(c))
+            // full, vector-aligned batches whose w range is proven safe (nearly
+            // all) skip the per-point range test and decode in pairs; the rest
+            // take the general body
+            if (LIST == 0 && (item & kItemWSafe) && count == kPointsPerBatch && (first & 3) == 0 &&
+                pair_batch_exact(c))
                 run_full10<MODE, PAYLOAD, BLOCK>(rd.y, bl, s_zc, c, pp, first, l0_x12);
             else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, pp, first, count, l0_x12);

@@ -207,6 +207,37 @@ def test_full_batch_with_tiny_extent(ctx, axis, payload):
     assert (got != L.DEFAULT_CLEAR).sum() > 20
 
 
+@pytest.mark.parametrize("case", ["w_crosses_zero", "w_above_2^120"])
+@pytest.mark.parametrize("method", [L.METHOD_LOOP_LAS, L.METHOD_LOOP_LAS_HQS])
+def test_full_batch_outside_the_safe_w_range(ctx, case, method):
+    """Full 10-bit batches whose clip w is not provably inside [2^-120, 2^120]
+    (the cull's w-safe flag is clear) take the general body with the checked
+    reciprocal; the result still matches the oracle."""
+    rng = np.random.default_rng(21)
+    pts = rng.integers(0, 1024, (10240, 3))
+    colors = rng.integers(1, 1 << 24, 10240)
+    if case == "w_crosses_zero":
+        lo, hi = (-0.25, -0.25, -0.5), (0.25, 0.25, 0.5)
+    else:
+        lo, hi = (-1e36, -1e36, 2e36), (1e36, 1e36, 4e36)
+    hm = handmade_cloud(pts, colors, box_min=lo, box_max=hi)
+    proj = np.eye(4)
+    proj[2, 3], proj[3, 3] = 1.0, 0.0  # column-major: w = z
+    cam = (np.eye(4).reshape(16), proj.reshape(16), 64, 32)
+    if method == L.METHOD_LOOP_LAS:
+        got, want = run_handmade(ctx, hm, cam, method, L.PAYLOAD_COLOR)
+        assert np.array_equal(got, want), first_diff(got, want)
+        assert (got != L.DEFAULT_CLEAR).sum() > 20
+        return
+    cloud = ctx.cloud_from_arrays(hm["batches"], hm["lo"], hm["md"], hm["hi"], hm["rgba"],
+                                  hm["box_min"])
+    fb, _ = gpu_raw(ctx, cloud, cam, method)
+    fr = oracle_frame(cam, hm["box_min"][None], QUIRKS[method])
+    depth, accum, _ = O.hqs(fr, hm["batches"], hm["n"], hm["lo"], hm["md"], hm["hi"], hm["rgba"])
+    assert np.array_equal(fb.read(L.FB_DEPTH), depth)
+    assert np.array_equal(fb.read(L.FB_ACCUM), accum)
+
+
 @pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
 def test_equal_depth_ties_take_min_payload(ctx, payload):
     pts = [(300, 300, 10)] * 40 + [(301, 300, 10)] * 3

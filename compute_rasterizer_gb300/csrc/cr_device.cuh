@@ -221,11 +221,14 @@ __device__ __forceinline__ void project_clip(const BatchCtx& c, float x, float y
     pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
 }
 
-// Divide, inside test and pixel (render.cs:402-409).
+// Divide, inside test and pixel (render.cs:402-409).  SAFE: the caller
+// guarantees w in [2^-120, 2^120] (w_safe), so the reciprocal needs no range
+// test.
+template <bool SAFE = false>
 __device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, float py, float pw,
                                                int32_t& pix, uint32_t& wbits) {
     // render.cs:402 `pos.xyz / pos.w`: one correctly rounded reciprocal of w
-    const float rw = rcp_rn(pw);
+    const float rw = SAFE ? rcp_rn_normal(pw) : rcp_rn(pw);
     float qx = fmul(px, rw), qy = fmul(py, rw);
     // render.cs:404 written positively, so a NaN position is outside (the
     // negated form would keep it and index the framebuffer with garbage)
@@ -238,11 +241,12 @@ __device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, floa
 }
 
 // Project a decoded point (render.cs:399-409 under the arithmetic contract).
+template <bool SAFE = false>
 __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, float z, int32_t& pix,
                                         uint32_t& wbits) {
     float px, py, pw;
     project_clip(c, x, y, z, px, py, pw);
-    return project_finish(c, px, py, pw, pix, wbits);
+    return project_finish<SAFE>(c, px, py, pw, pix, wbits);
 }
 
 // ---- packed fp32 pairs ------------------------------------------------------

@@ -75,10 +75,14 @@ __device__ __forceinline__ float rcp_rn(float x) {
 // T[3], T[7], T[11], T[15]).  w is linear, so over the AABB its extremes are at
 // corners; decoded points stay within a few ulps of the AABB and each FMA
 // rounds once, so a computed w differs from the corner range by far less than
-// 2^-16 of the largest term sum, the margin taken here.  A NaN or infinite
-// corner value fails the test.
+// 2^-16 of the largest term sum, the margin taken here.  The extents must be
+// finite: with an infinite one the decode step is infinite and a decoded
+// coordinate (so w) can be infinite although every corner is finite.  A NaN
+// or infinite corner value fails the test.
 __device__ __forceinline__ bool w_safe(const float* T, float mnx, float mny, float mnz, float mxx,
                                        float mxy, float mxz) {
+    if (!isfinite(fsub(mxx, mnx)) || !isfinite(fsub(mxy, mny)) || !isfinite(fsub(mxz, mnz)))
+        return false;
     float lo = 0.0f, hi = 0.0f, mag = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; k++) {

@@ -238,6 +238,22 @@ def test_full_batch_outside_the_safe_w_range(ctx, case, method):
     assert np.array_equal(fb.read(L.FB_ACCUM), accum)
 
 
+def test_full_batch_with_infinite_step(ctx):
+    """A batch whose x extent overflows float (-2e38 .. 2e38): the decode step
+    is infinite, so decoded x is inf or NaN; every clip coordinate then is
+    inf or NaN and no point is in view, in the oracle and on the GPU alike."""
+    rng = np.random.default_rng(5)
+    pts = rng.integers(0, 1024, (10240, 3))
+    hm = handmade_cloud(pts, rng.integers(1, 1 << 24, 10240), box_min=(-2e38, -0.5, 0.0),
+                        box_max=(2e38, 0.5, 1.0))
+    proj = np.eye(4)
+    proj[0, 0], proj[1, 0] = 0.0, 1.0  # column-major: clip x = y
+    proj[0, 3] = 1e-39  # w = 1e-39 * x + 1
+    cam = (np.eye(4).reshape(16), proj.reshape(16), 64, 32)
+    got, want = run_handmade(ctx, hm, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR)
+    assert np.array_equal(got, want), first_diff(got, want)
+
+
 @pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
 def test_equal_depth_ties_take_min_payload(ctx, payload):
     pts = [(300, 300, 10)] * 40 + [(301, 300, 10)] * 3

@@ -381,11 +381,14 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             const FileRec& f = vp.files[rd.y];
 
             BatchCtx c;
-            const float steps = level >= 2 ? 1024.0f : 1073741824.0f;
+            // render.cs:355-357, 392-394 boxSize / STEPS: a division by a power
+            // of two is the same real value as the product with its exact
+            // reciprocal, so both round alike for every input
+            const float inv = level >= 2 ? 0x1p-10f : 0x1p-30f;
             c.mnx = mnx; c.mny = mny; c.mnz = mnz;
-            c.sx = __fdiv_rn(fsub(mxx, mnx), steps);
-            c.sy = __fdiv_rn(fsub(mxy, mny), steps);
-            c.sz = __fdiv_rn(fsub(mxz, mnz), steps);
+            c.sx = fmul(fsub(mxx, mnx), inv);
+            c.sy = fmul(fsub(mxy, mny), inv);
+            c.sz = fmul(fsub(mxz, mnz), inv);
             c.T0 = f.T[0]; c.T1 = f.T[1]; c.T3 = f.T[3];
             c.T4 = f.T[4]; c.T5 = f.T[5]; c.T7 = f.T[7];
             c.T8 = f.T[8]; c.T9 = f.T[9]; c.T11 = f.T[11];

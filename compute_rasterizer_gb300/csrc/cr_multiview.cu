@@ -249,9 +249,10 @@ __device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
         const bool need12 = LIST == 1 && (classes & 1u) != 0;
         float sc[6];
         const float sx = fsub(mxx, mnx), sy = fsub(mxy, mny), sz = fsub(mxz, mnz);
-        sc[0] = __fdiv_rn(sx, 1024.0f); sc[1] = __fdiv_rn(sy, 1024.0f); sc[2] = __fdiv_rn(sz, 1024.0f);
-        sc[3] = __fdiv_rn(sx, 1073741824.0f); sc[4] = __fdiv_rn(sy, 1073741824.0f);
-        sc[5] = __fdiv_rn(sz, 1073741824.0f);
+        // size / 1024 and size / 2^30 as products with the exact reciprocals
+        // (the same real value, so the same rounding for every input)
+        sc[0] = fmul(sx, 0x1p-10f); sc[1] = fmul(sy, 0x1p-10f); sc[2] = fmul(sz, 0x1p-10f);
+        sc[3] = fmul(sx, 0x1p-30f); sc[4] = fmul(sy, 0x1p-30f); sc[5] = fmul(sz, 0x1p-30f);
 
         const int64_t v0 = first >> 2;
         const int32_t head = (int32_t)(first & 3);

@@ -146,7 +146,8 @@ int32_t cr_ctx_num_sms(const cr_ctx* ctx);
 enum { CR_STREAM_LOW = 1, CR_STREAM_MED = 2, CR_STREAM_HIG = 4, CR_STREAM_RGBA = 8, CR_STREAM_ALL = 15 };
 
 /* Allocates device storage for `num_points` points in `num_batches` records
- * across `num_files` files (per-file boxMin feeds the world matrix). */
+ * across `num_files` files (per-file boxMin feeds the world matrix).
+ * num_points < 2^31 - 64 and num_batches < 2^28 (cr_cloud_wrap alike). */
 cr_status cr_cloud_create(cr_ctx* ctx, int64_t num_points, int64_t num_batches, int32_t num_files,
                           int32_t stream_mask, cr_cloud** out);
 /* Host -> device copies (pinned or pageable).  Any stream pointer may be NULL

@@ -193,8 +193,9 @@ __device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, c
 // Points [first, first + count) are read as 128-bit vectors starting at the
 // aligned word below `first`; lanes mask the words outside the range.  The
 // next vector is loaded before the current one is processed.  PF >= 0 (full
-// 10-bit batches of file PF): points are decoded and projected in pairs with
-// the file's uniforms from the kernel parameters (project_pair10).
+// 10-bit batches of file PF that the cull flagged w-safe): points are decoded
+// and projected in pairs with the file's uniforms from the kernel parameters
+// and the unchecked reciprocal (project_pair10).
 template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false, int PF = -1>
 __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned long long* zc,
                                            const BatchCtx& c, const PairParams& pp, int64_t first,

@@ -23,7 +23,10 @@ OK, INVALID_ARG, OUT_OF_MEMORY, ADMISSION_REJECTED, TIMEOUT, CUDA_ERROR, DEVICE_
 METHOD_LOOP_LAS, METHOD_LOOP_LAS_PREFETCH, METHOD_LOOP_LAS_HQS, METHOD_EARLYZ, METHOD_DEDUP, \
     METHOD_EARLYZ_REDUCE = range(6)
 PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
-QUIRK_L0_X12, QUIRK_INCLUSIVE_END, QUIRK_DISPATCH_BY_POINTS = 1, 2, 4
+QUIRK_L0_X12, QUIRK_INCLUSIVE_END, QUIRK_DISPATCH_BY_POINTS, QUIRK_UVEC4_BASE, QUIRK_PLAIN_TILES = \
+    1, 2, 4, 8, 16
+MAX_FILES = 65536
+NOALLOC_MAX_BATCHES, NOALLOC_MAX_FILES, NOALLOC_SCRATCH_BYTES = 131064, 1024, 753664
 QUIRKS_METHOD_DEFAULT = -1
 STREAM_LOW, STREAM_MED, STREAM_HIG, STREAM_RGBA, STREAM_ALL = 1, 2, 4, 8, 15
 FB_U64, FB_HQS = 0, 1
@@ -167,6 +170,7 @@ _SIGS = {
     "cr_resolve": (I32, [P, P, C.POINTER(RenderParams), P, P]),
     "cr_render_batched_noalloc": (I32, [P, I64, I64, P, P, P, P, I64, P, I32, C.POINTER(View),
                                         C.POINTER(RenderParams), P, P]),
+    "cr_noalloc_scratch": (I32, [PP, C.POINTER(I64)]),
     "cr_mv_create": (I32, [P, P, I32, P, P, C.POINTER(RenderParams), PP]),
     "cr_mv_destroy": (I32, [P]),
     "cr_mv_last_error": (C.c_char_p, [P]),

@@ -47,8 +47,9 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
     """Compile and link libcr_raster.so; returns its path."""
     OUT.mkdir(parents=True, exist_ok=True)
     srcs = [CSRC / s for s in SOURCES]
-    deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "cr_raster.h",
-                                            PKG.parent / "include" / "cr_synth.h"]
+    # every header a source includes: the package's own and the public ones
+    deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + \
+        list((PKG.parent / "include").glob("*.h")) + list((PKG.parent / "include").glob("*.hpp"))
     if LIB.exists() and not force and not verbose_ptxas:
         newest = max(p.stat().st_mtime for p in deps if p.exists())
         if LIB.stat().st_mtime >= newest:

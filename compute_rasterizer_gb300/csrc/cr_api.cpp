@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "cr_filerec.h"
 #include "cr_internal.h"
 
 struct cr_frame_events {
@@ -27,6 +28,8 @@ struct cr_ctx {
     int num_sms = 0;
     uint32_t* scratch = nullptr;  // counters + work list
     int64_t scratch_words = 0;
+    cr::FileRec* files = nullptr;  // per-file records of the frame's view (clouds > 8 files)
+    int32_t files_cap = 0;
     int64_t last_dispatched = 0;  // batch records the last cull looked at
     std::vector<cr_frame_events> timing;  // GLTimerQueries-style event pairs
     int32_t timing_used = 0;
@@ -66,10 +69,6 @@ struct cr_fb {
     uint32_t* image = nullptr;
 };
 
-namespace cr {
-int batched_blocks_per_sm(int mode, int payload, int block);
-}
-
 namespace {
 
 using namespace cr;
@@ -96,61 +95,6 @@ cr_status cuda_fail(cr_ctx* ctx, cudaError_t e, const char* what) {
 
 // ---- host matrix setup ------------------------------------------------------
 
-// glm operator*(mat4, mat4): column c = A[0]*B[c][0] + A[1]*B[c][1] + A[2]*B[c][2] + A[3]*B[c][3]
-template <typename T>
-void mat_mul(const T* a, const T* b, T* out) {
-    T r[16];
-    for (int c = 0; c < 4; c++) {
-        for (int row = 0; row < 4; row++) {
-            T s = a[row] * b[c * 4];
-            s = s + a[4 + row] * b[c * 4 + 1];
-            s = s + a[8 + row] * b[c * 4 + 2];
-            s = s + a[12 + row] * b[c * 4 + 3];
-            r[c * 4 + row] = s;
-        }
-    }
-    std::memcpy(out, r, sizeof(r));
-}
-
-// render.cs:134-174: planes from the rows of transformFrustum, normalised.
-void frustum_planes(const float* m, float* planes) {
-    const float comb[6][4] = {
-        {m[3] - m[0], m[7] - m[4], m[11] - m[8], m[15] - m[12]},
-        {m[3] + m[0], m[7] + m[4], m[11] + m[8], m[15] + m[12]},
-        {m[3] + m[1], m[7] + m[5], m[11] + m[9], m[15] + m[13]},
-        {m[3] - m[1], m[7] - m[5], m[11] - m[9], m[15] - m[13]},
-        {m[3] - m[2], m[7] - m[6], m[11] - m[10], m[15] - m[14]},
-        {m[3] + m[2], m[7] + m[6], m[11] + m[10], m[15] + m[14]},
-    };
-    for (int i = 0; i < 6; i++) {
-        const float* p = comb[i];
-        float len = std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
-        // render.cs:139-140: vec3 / length is one reciprocal, w / length a division
-        const float inv = 1.0f / len;
-        planes[4 * i + 0] = p[0] * inv;
-        planes[4 * i + 1] = p[1] * inv;
-        planes[4 * i + 2] = p[2] * inv;
-        planes[4 * i + 3] = p[3] / len;
-    }
-}
-
-// compute_loop_las.h:166-200 for one file.
-void file_record(const double* view, const double* proj, const double* box_min, FileRec* out) {
-    const double world[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0,
-                              box_min[0], box_min[1], box_min[2], 1};
-    double pv[16], t[16];
-    mat_mul(proj, view, pv);
-    mat_mul(pv, world, t);
-    float fview[16], fworld[16];
-    for (int i = 0; i < 16; i++) {
-        out->T[i] = (float)t[i];
-        fview[i] = (float)view[i];
-        fworld[i] = (float)world[i];
-    }
-    frustum_planes(out->T, out->planes);
-    mat_mul(fview, fworld, out->VW);
-}
-
 bool finite_all(const double* v, int n) {
     for (int i = 0; i < n; i++)
         if (!std::isfinite(v[i])) return false;
@@ -161,17 +105,37 @@ cr_status build_view_params(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* v
                             ViewParams* vp) {
     if (!finite_all(view->view, 16) || !finite_all(view->proj, 16))
         return fail(ctx, CR_ERR_INVALID_ARG, "view matrices must be finite%s", "");
-    if (cloud->nfiles > kInlineFiles)
-        return fail(ctx, CR_ERR_UNSUPPORTED, "clouds with more than %s%lld files are not supported", "",
-                    (long long)kInlineFiles);
     std::memset(vp, 0, sizeof(*vp));
     for (int i = 0; i < 16; i++) vp->P[i] = (float)view->proj[i];
     vp->W = view->width;
     vp->H = view->height;
     vp->nfiles = cloud->nfiles;
     vp->culling = culling ? 1 : 0;
-    for (int f = 0; f < cloud->nfiles; f++)
+    for (int f = 0; f < std::min(cloud->nfiles, kInlineFiles); f++)
         file_record(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f]);
+    return CR_OK;
+}
+
+// Clouds with more than kInlineFiles files: every file's record of this view,
+// computed on the GPU on `stream` into the context's record array.
+cr_status enqueue_file_records(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
+                               ViewParams* vp, void* stream) {
+    if (cloud->nfiles <= kInlineFiles) return CR_OK;
+    if (ctx->files_cap < cloud->nfiles) {
+        if (ctx->files) {
+            // a frame still in flight may read the old array
+            CR_CUDA(ctx, cudaDeviceSynchronize(), "synchronize");
+            cudaFree(ctx->files);
+            ctx->files = nullptr;
+            ctx->files_cap = 0;
+        }
+        CR_CUDA(ctx, cudaMalloc(&ctx->files, sizeof(FileRec) * (size_t)cloud->nfiles), "file records");
+        ctx->files_cap = cloud->nfiles;
+    }
+    if (launch_file_records(view->view, view->proj, cloud->box_min.data(), cloud->nfiles, ctx->files,
+                            stream) != 0)
+        return fail(ctx, CR_ERR_CUDA, "file record launch failed%s", "");
+    vp->dfiles = ctx->files;
     return CR_OK;
 }
 
@@ -226,9 +190,13 @@ bool plain_method(int32_t m) {
 int default_quirks(int32_t method) {
     switch (method) {
         case CR_METHOD_LOOP_LAS: return CR_QUIRK_L0_X12;
-        case CR_METHOD_LOOP_LAS_PREFETCH: return CR_QUIRK_INCLUSIVE_END | CR_QUIRK_DISPATCH_BY_POINTS;
+        case CR_METHOD_LOOP_LAS_PREFETCH:
+            return CR_QUIRK_INCLUSIVE_END | CR_QUIRK_DISPATCH_BY_POINTS | CR_QUIRK_UVEC4_BASE;
         case CR_METHOD_LOOP_LAS_HQS:
             return CR_QUIRK_L0_X12 | CR_QUIRK_INCLUSIVE_END | CR_QUIRK_DISPATCH_BY_POINTS;
+        case CR_METHOD_EARLYZ:
+        case CR_METHOD_DEDUP:
+        case CR_METHOD_EARLYZ_REDUCE: return CR_QUIRK_PLAIN_TILES;
         default: return 0;
     }
 }
@@ -261,7 +229,7 @@ int cr::ctx_device(const cr_ctx* ctx) { return ctx ? ctx->device : 0; }
 
 cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
                               int32_t culling, ViewParams* vp) {
-    if (!view || !box_min || !vp || num_files < 1 || num_files > kInlineFiles)
+    if (!view || !box_min || !vp || num_files < 1 || num_files > kMaxFiles)
         return CR_ERR_INVALID_ARG;
     if (!finite_all(view->view, 16) || !finite_all(view->proj, 16) ||
         !finite_all(box_min, 3 * num_files))
@@ -272,7 +240,8 @@ cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_
     vp->H = view->height;
     vp->nfiles = num_files;
     vp->culling = culling ? 1 : 0;
-    for (int f = 0; f < num_files; f++) file_record(view->view, view->proj, &box_min[3 * f], &vp->files[f]);
+    for (int f = 0; f < std::min(num_files, kInlineFiles); f++)
+        file_record(view->view, view->proj, &box_min[3 * f], &vp->files[f]);
     return CR_OK;
 }
 
@@ -387,6 +356,7 @@ cr_status cr_ctx_destroy(cr_ctx* ctx) {
     if (!ctx) return CR_ERR_INVALID_ARG;
     destroy_timing(ctx);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->files) cudaFree(ctx->files);
     delete ctx;
     return CR_OK;
 }
@@ -396,7 +366,7 @@ const char* cr_last_error(const cr_ctx* ctx) { return ctx ? ctx->last_error.c_st
 int32_t cr_ctx_num_sms(const cr_ctx* ctx) { return ctx ? ctx->num_sms : 0; }
 
 cr_status cr_ctx_check(cr_ctx* ctx, void* stream) {
-    if (!ctx) return CR_ERR_INVALID_ARG;
+    if (!ctx) return noalloc_check(stream);
     CR_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream), "stream synchronize");
     uint32_t flag = 0;
     CR_CUDA(ctx, cudaMemcpy(&flag, ctx->scratch + kErrWord, 4, cudaMemcpyDeviceToHost), "flag read");
@@ -432,7 +402,7 @@ cr_status cr_cloud_create(cr_ctx* ctx, int64_t n, int64_t nb, int32_t nfiles, in
     if (!ctx || !out) return CR_ERR_INVALID_ARG;
     *out = nullptr;
     if (n < 0 || nb < 0 || nb >= kMaxBatches || n >= ((int64_t)1 << 31) - kStreamPad ||
-        nfiles < 1 || nfiles > kInlineFiles || (mask & CR_STREAM_LOW) == 0)
+        nfiles < 1 || nfiles > kMaxFiles || (mask & CR_STREAM_LOW) == 0)
         return fail(ctx, CR_ERR_INVALID_ARG, "bad cloud shape %s(n=%lld)", "", (long long)n);
     cr_cloud* c = new (std::nothrow) cr_cloud();
     if (!c) return CR_ERR_OUT_OF_MEMORY;
@@ -586,7 +556,7 @@ cr_status cr_cloud_wrap(cr_ctx* ctx, int64_t n, int64_t nb, int32_t nfiles, cons
                         const uint32_t* rgba, int64_t stream_words, cr_cloud** out) {
     if (!ctx || !out || !batches || !lo || n < 0 || nb < 0 || nb >= kMaxBatches ||
         n >= ((int64_t)1 << 31) ||
-        nfiles < 1 || nfiles > kInlineFiles || stream_words < n + kStreamPad)
+        nfiles < 1 || nfiles > kMaxFiles || stream_words < n + kStreamPad)
         return fail(ctx, CR_ERR_INVALID_ARG, "bad wrapped cloud arguments%s", "");
     *out = nullptr;
     const void* arrays[5] = {batches, lo, md, hi, rgba};
@@ -664,6 +634,9 @@ cr_status cr_fb_create(cr_ctx* ctx, int32_t W, int32_t H, int32_t kind, cr_fb** 
         if (e == cudaSuccess) e = cudaMalloc(&f->accum, (size_t)f->words * 16);
     }
     if (e == cudaSuccess) e = cudaMalloc(&f->image, (size_t)W * H * 4);
+    // a new image starts at zero: pixels a resolve does not cover (the plain
+    // methods' partial tiles) read back as 0, not as stale device memory
+    if (e == cudaSuccess) e = cudaMemset(f->image, 0, (size_t)W * H * 4);
     if (e != cudaSuccess) {
         cr_fb_destroy(ctx, f);
         return cuda_fail(ctx, e, "framebuffer allocation");
@@ -739,7 +712,10 @@ cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params*
     } else {
         if (fb->kind != CR_FB_U64) return fail(ctx, CR_ERR_INVALID_ARG, "method needs a u64 fb%s", "");
         if (plain_method(p->method)) {
-            rc = launch_resolve_plain(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value, stream);
+            const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? default_quirks(p->method) : p->quirks;
+            rc = launch_resolve_plain(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value,
+                                      (quirks & CR_QUIRK_PLAIN_TILES) != 0,
+                                      p->method != CR_METHOD_DEDUP, stream);
         } else if (p->payload == CR_PAYLOAD_COLOR) {
             rc = launch_resolve_color(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value, stream);
         } else {
@@ -821,7 +797,9 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
 
     ViewParams vp;
     s = build_view_params(ctx, cloud, view, p->frustum_culling, &vp);
+    if (s != CR_OK) return s;
     vp.lod_skip_level = p->lod_skip_level;
+    s = enqueue_file_records(ctx, cloud, view, &vp, stream);
     if (s != CR_OK) return s;
     // the loader's numBatchesLoaded / numPointsLoaded (compute_loop_las.h:233,
     // compute_loop_las2.h:234)
@@ -860,7 +838,9 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
             break;
         }
         bl.mode = modes[pass];
-        int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm : batched_blocks_per_sm(bl.mode, bl.payload, block);
+        int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm
+                                         : batched_blocks_per_sm(bl.mode, bl.payload, block,
+                                                                 cloud->nfiles > kInlineFiles);
         if (per_sm < 1) per_sm = 1;
         const int grid = ctx->num_sms * per_sm;
         if (launch_batched(vp, bl, block, grid, stream) != 0)

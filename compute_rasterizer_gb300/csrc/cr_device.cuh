@@ -12,6 +12,18 @@
 namespace cr {
 namespace {
 
+// Launches `k` and returns 0 when the launch itself was accepted.  The launch's
+// own status is checked, so an error left behind by other work in the
+// process is neither reported nor cleared here.
+template <typename... KArgs, typename... Args>
+int launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = s;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<Args&&>(args)...) == cudaSuccess ? 0 : -1;
+}
+
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint32_t kNoPixel = 0xFFFFFFFFu;
 
@@ -260,16 +272,19 @@ __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, flo
 // one instruction.  Two points of a lane go through the decode and the
 // projection side by side, which halves those float instructions on the
 // issue-bound raster without changing a bit of any result.  The uniforms the
-// pairs need, (u, u) for each uniform u, sit in the kernel parameters: with a
-// fixed file index every operand is a constant-bank operand and needs no
-// register.
-struct PairFile {
-    uint64_t T[12];  // (T[k], T[k]) for T0, T1, T3, T4, T5, T7, T8, T9, T11, T12, T13, T15
-};
+// pairs need are (u, u) for each uniform u.  A file's transform is proj * view
+// * translate(boxMin): its columns 0-2 are proj * view's, computed by the same
+// operations on the same operands for every file, so the nine pairs of those
+// columns are the same for all files and sit in the kernel parameters
+// (constant-bank operands, no registers); only column 3 (T12, T13, T15)
+// belongs to the batch's file and is held in registers per batch.
 struct PairParams {
-    PairFile files[kInlineFiles];
+    uint64_t T[9];          // (T[k], T[k]) for T0, T1, T3, T4, T5, T7, T8, T9, T11
     uint64_t half, Wf, Hf;  // (0.5, 0.5), (W, W), (H, H)
     uint64_t bias;          // (-2^23, -2^23)
+};
+struct PairCol3 {
+    uint64_t T12, T13, T15;  // the batch's file's translation column, as pairs
 };
 
 __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
@@ -348,7 +363,7 @@ __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, ui
 // are the same real numbers y*sy and z*sz, so each FMA rounds exactly as
 // fma(float(y), sy, min_y) does (measured 1.6 % faster on the color raster,
 // 3.9 % on the index one, than shift, mask and convert per field).
-__device__ __forceinline__ void project_pair10(const PairFile& f, const PairParams& pp,
+__device__ __forceinline__ void project_pair10(const PairParams& pp, const PairCol3& f,
                                                const PairBatch& b, int32_t W, uint32_t a0,
                                                uint32_t a1, bool ok[2], int32_t pix[2],
                                                uint32_t wbits[2]) {
@@ -361,23 +376,23 @@ __device__ __forceinline__ void project_pair10(const PairFile& f, const PairPara
     const uint64_t X = f2_fma(XF, b.sx, b.mnx);
     const uint64_t Y = f2_fma(YF, b.sy, b.mny);
     const uint64_t Z = f2_fma(ZF, b.sz, b.mnz);
-    // project_clip: T0 T1 T3 T4 T5 T7 T8 T9 T11 T12 T13 T15 are T[0..11]
-    const uint64_t PX = f2_fma(f.T[6], Z, f2_fma(f.T[3], Y, f2_fma(f.T[0], X, f.T[9])));
-    const uint64_t PY = f2_fma(f.T[7], Z, f2_fma(f.T[4], Y, f2_fma(f.T[1], X, f.T[10])));
-    const uint64_t PW = f2_fma(f.T[8], Z, f2_fma(f.T[5], Y, f2_fma(f.T[2], X, f.T[11])));
+    // project_clip: T0 T1 T3 T4 T5 T7 T8 T9 T11 are pp.T[0..8]
+    const uint64_t PX = f2_fma(pp.T[6], Z, f2_fma(pp.T[3], Y, f2_fma(pp.T[0], X, f.T12)));
+    const uint64_t PY = f2_fma(pp.T[7], Z, f2_fma(pp.T[4], Y, f2_fma(pp.T[1], X, f.T13)));
+    const uint64_t PW = f2_fma(pp.T[8], Z, f2_fma(pp.T[5], Y, f2_fma(pp.T[2], X, f.T15)));
     project_pair_finish(PX, PY, PW, pp.half, pp.Wf, pp.Hf, W, ok, pix, wbits);
 }
 
-// Host side: the pair uniforms of every file of a view.
+// Host side: the pair uniforms of a view (file 0's columns 0-2, which every
+// file shares).
 inline void fill_pair_params(const ViewParams& vp, PairParams* pp) {
     auto dup = [](float f) {
         uint32_t u;
         __builtin_memcpy(&u, &f, 4);
         return ((uint64_t)u << 32) | u;
     };
-    static const int kIdx[12] = {0, 1, 3, 4, 5, 7, 8, 9, 11, 12, 13, 15};
-    for (int f = 0; f < kInlineFiles; f++)
-        for (int k = 0; k < 12; k++) pp->files[f].T[k] = dup(vp.files[f].T[kIdx[k]]);
+    static const int kIdx[9] = {0, 1, 3, 4, 5, 7, 8, 9, 11};
+    for (int k = 0; k < 9; k++) pp->T[k] = dup(vp.files[0].T[kIdx[k]]);
     pp->half = dup(0.5f);
     pp->bias = dup(-8388608.0f);
     pp->Wf = dup((float)vp.W);

@@ -22,6 +22,7 @@ struct NvtxRange {
 
 constexpr int kPointsPerBatch = CR_POINTS_PER_BATCH;
 constexpr int kInlineFiles = 8;       // per-file records passed in kernel parameters
+constexpr int32_t kMaxFiles = CR_MAX_FILES;  // files per cloud (records in device memory past 8)
 constexpr uint32_t kBackground = 0x00443322u;  // resolve.cs:141
 constexpr uint64_t kDefaultClear = 0xFF800000FF800000ull;  // compute_loop_las.h:292-296
 constexpr uint64_t kPlainReclear = 0xffffffffff3c321eull;  // compute_2021_earlyz/resolve.cs:77
@@ -51,6 +52,9 @@ struct FileRec {
     float VW[16];      // uniforms.view * file.world (float product)
 };
 
+// Files [0, kInlineFiles) have their records in the kernel parameters; with
+// more files, `dfiles` holds every file's record in device memory and files
+// from kInlineFiles on are read from there (file_rec()).
 struct ViewParams {
     float P[16];       // uniforms.proj
     int32_t W, H;
@@ -58,6 +62,7 @@ struct ViewParams {
     int32_t culling;
     int32_t lod_skip_level;  // >0: batches at level >= this are not rendered
     FileRec files[kInlineFiles];
+    const FileRec* dfiles;   // nfiles records when nfiles > kInlineFiles, else null
 };
 
 // Scratch words at the head of the ctx scratch buffer.  The cull kernel sorts
@@ -96,6 +101,11 @@ struct BatchedLaunch {
 };
 
 // Host-callable launchers (cr_kernels.cu).
+// Every file's record for one view, computed on the GPU from the double
+// matrices and the files' boxMin (host array, passed to the kernels in their
+// parameters, 1024 files per launch) into out[0, nfiles).
+int launch_file_records(const double view[16], const double proj[16], const double* box_min,
+                        int32_t nfiles, FileRec* out, void* stream);
 int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb_dispatch,
                 int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream);
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
@@ -108,8 +118,10 @@ int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgb
                          void* stream);
 int launch_resolve_color(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
                          uint64_t clear, void* stream);
+// tiles: CR_QUIRK_PLAIN_TILES; zero_rule: ucol == 0 resolves to opaque black
+// (early-z, early-z & reduce; not dedup)
 int launch_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
-                         uint64_t clear, void* stream);
+                         uint64_t clear, int tiles, int zero_rule, void* stream);
 int launch_resolve_hqs(int32_t W, int32_t H, uint32_t* depth, uint64_t* accum, uint32_t* image,
                        int clear_after, void* stream);
 int launch_fill_u64(uint64_t* p, int64_t n, uint64_t v, void* stream);
@@ -117,9 +129,12 @@ int launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, void* stream);
 // rcp_rn against __frcp_rn over every float; counts into bad[0], the lowest
 // mismatching bit pattern into *first (synchronous, default stream).
 int launch_check_reciprocal(uint64_t* bad, uint32_t* first);
-int batched_blocks_per_sm(int mode, int payload, int block);
+// many: the cloud has more than kInlineFiles files (its own kernel instances)
+int batched_blocks_per_sm(int mode, int payload, int block, bool many = false);
 
-// Per-view uniforms from double matrices and per-file boxMin (cr_api.cpp).
+// Per-view uniforms from double matrices and per-file boxMin (cr_api.cpp):
+// the records of the first min(num_files, kInlineFiles) files; dfiles is left
+// null and must be set by the caller when num_files > kInlineFiles.
 cr_status view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
                           int32_t culling, ViewParams* out);
 
@@ -138,6 +153,8 @@ struct CloudInfo {
 };
 bool cloud_info(const cr_cloud* cloud, CloudInfo* out);
 int default_quirks_for(int32_t method);
+// cr_ctx_check(NULL, stream): the no-alloc array's error flag (cr_noalloc.cu)
+cr_status noalloc_check(void* stream);
 int ctx_device(const cr_ctx* ctx);
 
 // ---- multi-view frames (cr_multiview.cu), shared by cr_mv plans and the server
@@ -157,8 +174,10 @@ struct MVView {
     uint32_t img_off;  // u32 offset of the view's image from MVFrame::images
 };
 
-// Fills a view's P, W, H and its nfiles per-file records from the double
-// matrices (the single-view uniforms, so each view renders as cr_render would).
+// Fills a view's P, W, H and, for clouds of at most kInlineFiles files, its
+// per-file records from the double matrices (the single-view uniforms, so each
+// view renders as cr_render would).  With more files the records are computed
+// on the GPU each frame (MVFrame::d_mats, d_box) and out_files is not used.
 cr_status mv_fill_view(const cr_view* view, const CloudInfo& ci, MVView* out_view,
                        MVFile* out_files);
 
@@ -177,6 +196,11 @@ struct MVFrame {
     int32_t resolve, clear_after;
     uint64_t clear_value;
     int64_t max_words;       // max over the views of W*H+W+1
+    // clouds with more than kInlineFiles files: per view the double view and
+    // proj matrices (32 doubles), per file boxMin (3 doubles), both in device
+    // memory; the frame computes d_files from them before the cull
+    const double* d_mats;
+    const double* d_box;
 };
 int64_t mv_scratch_words(int64_t nb, int64_t nviews);
 // Enqueues counter reset, [fill], cull, raster (both lists), [resolve] on stream.

@@ -34,15 +34,50 @@
 
 #include "cr_internal.h"
 #include "cr_device.cuh"
+#include "cr_filerec.h"
 
 namespace cr {
 
 namespace {
 
+// ---- per-file records of one view (clouds with more than kInlineFiles files)
+
+constexpr int kFilesPerLaunch = 1024;
+struct FileChunk {
+    double view[16], proj[16];
+    int32_t first, count;
+    double box_min[3 * kFilesPerLaunch];
+};
+static_assert(sizeof(FileChunk) < 32000, "kernel parameters are limited to 32 KB");
+
+__global__ void __launch_bounds__(128) k_file_records(const __grid_constant__ FileChunk c,
+                                                      FileRec* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.count) return;
+    FileRec r;
+    file_record(c.view, c.proj, &c.box_min[3 * i], &r);
+    out[c.first + i] = r;
+}
+
+// The record of file `fi`: kernel parameters for the first kInlineFiles files,
+// the device array beyond (filled by k_file_records for this view).
+__device__ __forceinline__ const FileRec* file_rec(const ViewParams& vp, int fi) {
+    return fi < kInlineFiles ? &vp.files[fi] : vp.dfiles + fi;
+}
+
+// The 12 transform entries the projection uses (render.cs:399-401).
+__device__ __forceinline__ void load_transform(const float* T, BatchCtx& c) {
+    c.T0 = T[0]; c.T1 = T[1]; c.T3 = T[3];
+    c.T4 = T[4]; c.T5 = T[5]; c.T7 = T[7];
+    c.T8 = T[8]; c.T9 = T[9]; c.T11 = T[11];
+    c.T12 = T[12]; c.T13 = T[13]; c.T15 = T[15];
+}
+
 // ---- cull + level: one thread per batch record -----------------------------
 
-__global__ void __launch_bounds__(256) k_cull(ViewParams vp, const cr_batch* __restrict__ batches,
-                                              int64_t nb, int64_t capacity, int32_t quirks,
+__global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams vp,
+                                              const cr_batch* __restrict__ batches, int64_t nb,
+                                              int64_t capacity, int32_t quirks,
                                               uint32_t* __restrict__ scratch) {
     int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
@@ -59,7 +94,7 @@ __global__ void __launch_bounds__(256) k_cull(ViewParams vp, const cr_batch* __r
         if (!ok) {
             atomicOr(&scratch[kErrWord], kErrBadBatch);
         } else if (count > 0) {
-            const FileRec& f = vp.files[fi];
+            const FileRec& f = *file_rec(vp, fi);
             bool vis = !vp.culling || intersects_frustum(f.planes, mnx, mny, mnz, mxx, mxy, mxz);
             if (vis) {
                 int level = precision_level(vp.P, f.VW, vp.W, vp.H, mnx, mny, mnz, mxx, mxy, mxz);
@@ -192,19 +227,28 @@ __device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, c
 // LC: 2 = 10 bit (levels 2-4), 1 = 20 bit (level 1), 0 = 30 bit (level 0).
 // Points [first, first + count) are read as 128-bit vectors starting at the
 // aligned word below `first`; lanes mask the words outside the range.  The
-// next vector is loaded before the current one is processed.  PF >= 0 (full
-// 10-bit batches of file PF that the cull flagged w-safe): points are decoded
-// and projected in pairs with the file's uniforms from the kernel parameters
-// and the unchecked reciprocal (project_pair10).
-template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false, int PF = -1>
+// next vector is loaded before the current one is processed.  PAIRS (full
+// 10-bit batches that the cull flagged w-safe): points are decoded and
+// projected two at a time with the unchecked reciprocal (project_pair10).
+template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false, bool PAIRS = false>
 __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned long long* zc,
                                            const BatchCtx& c, const PairParams& pp, int64_t first,
                                            int32_t count, bool l0_x12) {
-    static_assert(PF < 0 || (FULL && LC == 2), "pairs decode full 10-bit batches");
+    static_assert(!PAIRS || (FULL && LC == 2), "pairs decode full 10-bit batches");
+    PairCol3 pf{};
+    if constexpr (PAIRS) pf = PairCol3{f2_pack(c.T12, c.T12), f2_pack(c.T13, c.T13), f2_pack(c.T15, c.T15)};
     constexpr bool kNeedColor = (MODE == kModeHqsColor) || (MODE == kModeRaster && PAYLOAD == CR_PAYLOAD_COLOR);
     const int64_t v0 = first >> 2;
     const int32_t head = (int32_t)(first & 3);
-    const int nv = (head + count + 3) >> 2;
+    // las2/render.cs:319-341 (CR_QUIRK_UVEC4_BASE, batches with firstPoint % 4 != 0):
+    // the reference's 128 threads read vectors 0..2559 from firstPoint / 4, so
+    // vector v's word j is batch point 4v + j - head; thread 0 (vectors v with
+    // v % 128 == 0) underflows its first localIndex and returns, and vectors past
+    // 2559 are never read.  Full batches start aligned (head == 0), where the
+    // addressing is the same as here.  Only the raster reads this way (HQS
+    // passes walk their batches with stride 128, hqs/depth.cs:270-276).
+    const bool uvec4 = MODE == kModeRaster && !FULL && head != 0 && (bl.quirks & CR_QUIRK_UVEC4_BASE) != 0;
+    const int nv = uvec4 ? min((head + count + 3) >> 2, kPointsPerBatch / 4) : (head + count + 3) >> 2;
     const uint32_t index0 = (uint32_t)(first - head);  // global index of word 0 of vector v0
     const uint4* lo4 = reinterpret_cast<const uint4*>(bl.lo) + v0;
     const uint4* md4 = reinterpret_cast<const uint4*>(bl.md) + v0;
@@ -213,7 +257,7 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
     const uint4 zero = make_uint4(0, 0, 0, 0);
     uint4 n4 = zero, n8 = zero, n12 = zero, ncol = zero;
     PairBatch pb{};
-    if constexpr (PF >= 0) pb = pair_batch(c);
+    if constexpr (PAIRS) pb = pair_batch(c);
     if ((int)threadIdx.x < nv) {
         n4 = ld_stream(lo4 + threadIdx.x);
         if (LC <= 1) n8 = ld_stream(md4 + threadIdx.x);
@@ -231,6 +275,8 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             if (kNeedColor) ncol = ld_stream(co4 + vn);
         }
         const int32_t rel0 = 4 * v - head;  // batch-local index of word 0
+        // the reference's thread 0 returns before any point when head != 0
+        const bool lane_live = !uvec4 || (v & 127) != 0;
         if constexpr (MODE == kModeHqsColor) {
             // The lane's 4 consecutive points, in runs of in-view points on one
             // pixel (Morton order puts most of them on the same pixel): project
@@ -240,13 +286,13 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             int32_t pix[4];
             uint32_t wb[4];
             bool ok[4];
-            if constexpr (PF >= 0) {
-                project_pair10(pp.files[PF], pp, pb, c.W, w4.x, w4.y, ok, pix, wb);
-                project_pair10(pp.files[PF], pp, pb, c.W, w4.z, w4.w, ok + 2, pix + 2, wb + 2);
+            if constexpr (PAIRS) {
+                project_pair10(pp, pf, pb, c.W, w4.x, w4.y, ok, pix, wb);
+                project_pair10(pp, pf, pb, c.W, w4.z, w4.w, ok + 2, pix + 2, wb + 2);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
+                    const bool valid = FULL || ((uint32_t)(rel0 + j) < (uint32_t)count && lane_live);
                     float x, y, z;
                     decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
                     ok[j] = project(c, x, y, z, pix[j], wb[j]) && valid;
@@ -281,14 +327,13 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
                 }
             }
             hqs_color_flush(bl, ok[3] && bc != 0u, pix[3], rg, bc);
-        } else if constexpr (PF >= 0) {
+        } else if constexpr (PAIRS) {
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 int32_t pix[2];
                 uint32_t wb[2];
                 bool ok[2];
-                project_pair10(pp.files[PF], pp, pb, c.W, h ? w4.z : w4.x, h ? w4.w : w4.y, ok,
-                               pix, wb);
+                project_pair10(pp, pf, pb, c.W, h ? w4.z : w4.x, h ? w4.w : w4.y, ok, pix, wb);
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
                     const int j = 2 * h + k;
@@ -301,7 +346,7 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
         } else {
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const bool valid = FULL || (uint32_t)(rel0 + j) < (uint32_t)count;
+                const bool valid = FULL || ((uint32_t)(rel0 + j) < (uint32_t)count && lane_live);
                 const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
                 float x, y, z;
                 decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
@@ -316,31 +361,11 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
     }
 }
 
-// Files whose full 10-bit batches take the paired body, one instance per file.
-// The HQS color pass pairs file 0 only: with more instances its register count
-// goes far past the 48 at which 10 CTAs of 128 threads stay resident per SM.
-template <int MODE>
-constexpr int kPairedFiles = MODE == kModeHqsColor ? 1 : kInlineFiles;
-// The HQS color pass's 10-bit instance is held to those 48 registers (its
-// uncapped 51 leave 9 CTAs per SM; measured 1 % slower).
+// The HQS color pass's 10-bit instance is held to 48 registers, at which 10
+// CTAs of 128 threads stay resident per SM (its uncapped 51 leave 9 CTAs per
+// SM; measured 1 % slower).
 template <int MODE, int BLOCK, int LIST>
 constexpr int kMinBlocks = MODE == kModeHqsColor && LIST == 0 ? 1280 / BLOCK : 0;
-
-// A full, vector-aligned 10-bit batch of file `fi`: the paired body with the
-// file's uniforms at a fixed parameter offset, or the scalar one.
-template <int MODE, int PAYLOAD, int BLOCK, int F = 0>
-__device__ __forceinline__ void run_full10(int fi, const BatchedLaunch& bl, unsigned long long* zc,
-                                           const BatchCtx& c, const PairParams& pp, int64_t first,
-                                           bool l0_x12) {
-    if constexpr (F < kPairedFiles<MODE>) {
-        if (fi == F)
-            run_points<MODE, PAYLOAD, BLOCK, 2, true, F>(bl, zc, c, pp, first, kPointsPerBatch, l0_x12);
-        else
-            run_full10<MODE, PAYLOAD, BLOCK, F + 1>(fi, bl, zc, c, pp, first, l0_x12);
-    } else {
-        run_points<MODE, PAYLOAD, BLOCK, 2, true>(bl, zc, c, pp, first, kPointsPerBatch, l0_x12);
-    }
-}
 
 // LIST 0: the 10-bit items (front of the list region), LIST 1: the 20/30-bit
 // items (back of the region).  Each list runs in its own instance, so the
@@ -348,7 +373,9 @@ __device__ __forceinline__ void run_full10(int fi, const BatchedLaunch& bl, unsi
 // List 1 is launched first and lets the list-0 grid start at once
 // (programmatic dependent launch); every list-0 CTA waits for the list-1 grid
 // before it exits, so work that follows on the stream sees both lists' writes.
-template <int MODE, int PAYLOAD, int BLOCK, int LIST>
+// MANY: the cloud has more than kInlineFiles files, whose records are read
+// from vp.dfiles (a separate instance, so the common case's code is untouched).
+template <int MODE, int PAYLOAD, int BLOCK, int LIST, bool MANY>
 __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
     k_batched(ViewParams vp, BatchedLaunch bl, PairParams pp) {
     if (LIST == 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -379,8 +406,6 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
             const int64_t first = rd.x;
             const int32_t count = (int32_t)points_in_batch(rc.w, bl.quirks);
-            const FileRec& f = vp.files[rd.y];
-
             BatchCtx c;
             // render.cs:355-357, 392-394 boxSize / STEPS: a division by a power
             // of two is the same real value as the product with its exact
@@ -390,10 +415,12 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             c.sx = fmul(fsub(mxx, mnx), inv);
             c.sy = fmul(fsub(mxy, mny), inv);
             c.sz = fmul(fsub(mxz, mnz), inv);
-            c.T0 = f.T[0]; c.T1 = f.T[1]; c.T3 = f.T[3];
-            c.T4 = f.T[4]; c.T5 = f.T[5]; c.T7 = f.T[7];
-            c.T8 = f.T[8]; c.T9 = f.T[9]; c.T11 = f.T[11];
-            c.T12 = f.T[12]; c.T13 = f.T[13]; c.T15 = f.T[15];
+            if constexpr (MANY) {
+                load_transform(vp.dfiles[rd.y].T, c);
+            } else {
+                const FileRec& f = vp.files[rd.y];
+                load_transform(f.T, c);
+            }
             c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
             const bool l0_x12 = (bl.quirks & CR_QUIRK_L0_X12) != 0;
             // full, vector-aligned batches whose w range is proven safe (nearly
@@ -401,7 +428,8 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             // take the general body
             if (LIST == 0 && (item & kItemWSafe) && count == kPointsPerBatch && (first & 3) == 0 &&
                 pair_batch_exact(c))
-                run_full10<MODE, PAYLOAD, BLOCK>(rd.y, bl, s_zc, c, pp, first, l0_x12);
+                run_points<MODE, PAYLOAD, BLOCK, 2, true, true>(bl, s_zc, c, pp, first,
+                                                                kPointsPerBatch, l0_x12);
             else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, pp, first, count, l0_x12);
             else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, pp, first, count, l0_x12);
@@ -544,19 +572,33 @@ __global__ void k_resolve_color(int64_t P, int64_t tail, uint64_t* __restrict__ 
 // uvec4(255.0 * unpackUnorm4x8(ucol)) per byte is trunc(255 * RN(c / 255)),
 // which is c again for every byte c (checked over all 256 values, the CPU
 // test test_plain_byte_round_trip), so the image word is ucol itself.
-__device__ __forceinline__ uint32_t plain_rgba8(uint64_t v) {
+// early-z and early-z & reduce map ucol == 0 to opaque black (resolve.cs:44-46);
+// the dedup resolve has no such rule (compute_2021_dedup/resolve.cs:15-21).
+__device__ __forceinline__ uint32_t plain_rgba8(uint64_t v, int zero_rule) {
     const uint32_t ucol = (uint32_t)(v & 0x00FFFFFFull);
-    return ucol == 0u ? 0xFF000000u : ucol;
+    return ucol == 0u && zero_rule ? 0xFF000000u : ucol;
 }
 
-__global__ void k_resolve_plain(int64_t P, int64_t tail, uint64_t* __restrict__ fb,
+// tiles != 0 (CR_QUIRK_PLAIN_TILES): only the pixels of the floor(W/16) x
+// floor(H/16) tiles of 16x16 that the reference dispatches
+// (compute_2021_earlyz.h:161-163) are resolved and re-cleared; every other
+// image and framebuffer word, the guard tail included, keeps its value.
+__global__ void k_resolve_plain(int64_t P, int64_t tail, int32_t W, int32_t H, int tiles,
+                                int zero_rule, uint64_t* __restrict__ fb,
                                 uint32_t* __restrict__ image, int clear_after, uint64_t clear) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < P) {
-        image[t] = plain_rgba8(fb[t]);
-        if (clear_after) fb[t] = clear;
+        bool covered = true;
+        if (tiles) {
+            const int64_t y = t / W, x = t - y * W;
+            covered = x < (W & ~15) && y < (H & ~15);
+        }
+        if (covered) {
+            image[t] = plain_rgba8(fb[t], zero_rule);
+            if (clear_after) fb[t] = clear;
+        }
     }
-    if (clear_after && t < tail) fb[P + t] = clear;
+    if (clear_after && !tiles && t < tail) fb[P + t] = clear;
 }
 
 // compute_loop_las_hqs/resolve.cs:62-130
@@ -611,24 +653,40 @@ __global__ void __launch_bounds__(256) k_check_reciprocal(unsigned long long* ba
 
 inline int blocks_for(int64_t n, int per) { return (int)((n + per - 1) / per); }
 
-int launch_status() { return cudaGetLastError() == cudaSuccess ? 0 : -1; }
-
 }  // namespace
+
+int launch_file_records(const double view[16], const double proj[16], const double* box_min,
+                        int32_t nfiles, FileRec* out, void* stream) {
+    // the chunk travels by value in the kernel parameters: no staging buffer
+    // whose lifetime would have to outlast the launch
+    static thread_local FileChunk c;
+    for (int i = 0; i < 16; i++) {
+        c.view[i] = view[i];
+        c.proj[i] = proj[i];
+    }
+    for (int32_t first = 0; first < nfiles; first += kFilesPerLaunch) {
+        c.first = first;
+        c.count = std::min<int32_t>(kFilesPerLaunch, nfiles - first);
+        for (int k = 0; k < 3 * c.count; k++) c.box_min[k] = box_min[3 * (int64_t)first + k];
+        if (launch_k(k_file_records, blocks_for(c.count, 128), 128, (cudaStream_t)stream, c, out) != 0)
+            return -1;
+    }
+    return 0;
+}
 
 int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb, int64_t capacity,
                 int32_t quirks, uint32_t* scratch, void* stream) {
     if (nb <= 0) return 0;
-    k_cull<<<blocks_for(nb, 256), 256, 0, (cudaStream_t)stream>>>(vp, batches, nb, capacity,
-                                                                   quirks, scratch);
-    return launch_status();
+    return launch_k(k_cull, blocks_for(nb, 256), 256, (cudaStream_t)stream, vp, batches, nb,
+                    capacity, quirks, scratch);
 }
 
-template <int MODE, int PAYLOAD, int BLOCK>
+template <int MODE, int PAYLOAD, int BLOCK, bool MANY>
 static int occupancy_list1() {
     static const int n = [] {
         int k = 0;
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_batched<MODE, PAYLOAD, BLOCK, 1>,
-                                                             BLOCK, 0) == cudaSuccess && k > 0
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &k, k_batched<MODE, PAYLOAD, BLOCK, 1, MANY>, BLOCK, 0) == cudaSuccess && k > 0
                    ? k
                    : 1;
     }();
@@ -638,15 +696,16 @@ static int occupancy_list1() {
 // The (usually short) 20/30-bit list with a grid that is resident at once,
 // then the 10-bit list as its programmatic dependent: it starts as soon as
 // every list-1 CTA has started, on the SM room list 1 leaves.
-template <int MODE, int PAYLOAD, int BLOCK>
-static void launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid, cudaStream_t s) {
+template <int MODE, int PAYLOAD, int BLOCK, bool MANY>
+static int launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid, cudaStream_t s) {
     int device = 0, sms = 1;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const int grid1 = std::min(grid, sms * occupancy_list1<MODE, PAYLOAD, BLOCK>());
+    if (cudaGetDevice(&device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return -1;
+    const int grid1 = std::min(grid, sms * occupancy_list1<MODE, PAYLOAD, BLOCK, MANY>());
     PairParams pp;
     fill_pair_params(vp, &pp);
-    k_batched<MODE, PAYLOAD, BLOCK, 1><<<grid1, BLOCK, 0, s>>>(vp, bl, pp);
+    if (launch_k(k_batched<MODE, PAYLOAD, BLOCK, 1, MANY>, grid1, BLOCK, s, vp, bl, pp) != 0) return -1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(BLOCK);
@@ -657,50 +716,56 @@ static void launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0>, vp, bl, pp);
+    return cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0, MANY>, vp, bl, pp) == cudaSuccess
+               ? 0
+               : -1;
 }
 
 template <int MODE, int PAYLOAD>
-static void launch_batched_t(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
-                             cudaStream_t s) {
+static int launch_batched_t(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
+                            cudaStream_t s) {
+    // clouds with more than kInlineFiles files: 128-thread instances only
+    if (vp.nfiles > kInlineFiles) return launch_lists<MODE, PAYLOAD, 128, true>(vp, bl, grid, s);
     switch (block) {
-        case 128: launch_lists<MODE, PAYLOAD, 128>(vp, bl, grid, s); break;
-        case 512: launch_lists<MODE, PAYLOAD, 512>(vp, bl, grid, s); break;
-        default: launch_lists<MODE, PAYLOAD, 256>(vp, bl, grid, s); break;
+        case 128: return launch_lists<MODE, PAYLOAD, 128, false>(vp, bl, grid, s);
+        case 512: return launch_lists<MODE, PAYLOAD, 512, false>(vp, bl, grid, s);
+        default: return launch_lists<MODE, PAYLOAD, 256, false>(vp, bl, grid, s);
     }
 }
 
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (bl.mode == kModeRaster) {
-        if (bl.payload == CR_PAYLOAD_COLOR) launch_batched_t<kModeRaster, CR_PAYLOAD_COLOR>(vp, bl, block, grid, s);
-        else launch_batched_t<kModeRaster, CR_PAYLOAD_INDEX>(vp, bl, block, grid, s);
-    } else if (bl.mode == kModeHqsDepth) {
-        launch_batched_t<kModeHqsDepth, CR_PAYLOAD_INDEX>(vp, bl, block, grid, s);
-    } else {
-        launch_batched_t<kModeHqsColor, CR_PAYLOAD_INDEX>(vp, bl, block, grid, s);
+        if (bl.payload == CR_PAYLOAD_COLOR)
+            return launch_batched_t<kModeRaster, CR_PAYLOAD_COLOR>(vp, bl, block, grid, s);
+        return launch_batched_t<kModeRaster, CR_PAYLOAD_INDEX>(vp, bl, block, grid, s);
     }
-    return launch_status();
+    if (bl.mode == kModeHqsDepth) return launch_batched_t<kModeHqsDepth, CR_PAYLOAD_INDEX>(vp, bl, block, grid, s);
+    return launch_batched_t<kModeHqsColor, CR_PAYLOAD_INDEX>(vp, bl, block, grid, s);
 }
 
 template <int MODE, int PAYLOAD>
-static int occupancy_t(int block) {
+static int occupancy_t(int block, bool many) {
     int n = 0;
     cudaError_t e;
+    if (many) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0, true>, 128, 0);
+        return e == cudaSuccess ? n : 1;
+    }
     switch (block) {
-        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0>, 128, 0); break;
-        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 512, 0>, 512, 0); break;
-        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 256, 0>, 256, 0); break;
+        case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0, false>, 128, 0); break;
+        case 512: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 512, 0, false>, 512, 0); break;
+        default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 256, 0, false>, 256, 0); break;
     }
     return e == cudaSuccess ? n : 1;
 }
 
-int batched_blocks_per_sm(int mode, int payload, int block) {
+int batched_blocks_per_sm(int mode, int payload, int block, bool many) {
     if (mode == kModeRaster)
-        return payload == CR_PAYLOAD_COLOR ? occupancy_t<kModeRaster, CR_PAYLOAD_COLOR>(block)
-                                           : occupancy_t<kModeRaster, CR_PAYLOAD_INDEX>(block);
-    if (mode == kModeHqsDepth) return occupancy_t<kModeHqsDepth, CR_PAYLOAD_INDEX>(block);
-    return occupancy_t<kModeHqsColor, CR_PAYLOAD_INDEX>(block);
+        return payload == CR_PAYLOAD_COLOR ? occupancy_t<kModeRaster, CR_PAYLOAD_COLOR>(block, many)
+                                           : occupancy_t<kModeRaster, CR_PAYLOAD_INDEX>(block, many);
+    if (mode == kModeHqsDepth) return occupancy_t<kModeHqsDepth, CR_PAYLOAD_INDEX>(block, many);
+    return occupancy_t<kModeHqsColor, CR_PAYLOAD_INDEX>(block, many);
 }
 
 int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
@@ -714,10 +779,9 @@ int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, in
     if (need < grid) grid = (int)need;
     const uint4* v4 = reinterpret_cast<const uint4*>(v);
     cudaStream_t s = (cudaStream_t)stream;
-    if (variant == 1) k_plain<256, 1><<<grid, 256, 0, s>>>(pp, v4, n, fb);
-    else if (variant == 2) k_plain<256, 2><<<grid, 256, 0, s>>>(pp, v4, n, fb);
-    else k_plain<256, 0><<<grid, 256, 0, s>>>(pp, v4, n, fb);
-    return launch_status();
+    if (variant == 1) return launch_k(k_plain<256, 1>, grid, 256, s, pp, v4, n, fb);
+    if (variant == 2) return launch_k(k_plain<256, 2>, grid, 256, s, pp, v4, n, fb);
+    return launch_k(k_plain<256, 0>, grid, 256, s, pp, v4, n, fb);
 }
 
 int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgba,
@@ -725,44 +789,42 @@ int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgb
                          void* stream) {
     int64_t P = (int64_t)W * H, tail = (int64_t)W + 1;
     int64_t threads = (P + 1) / 2 > tail ? (P + 1) / 2 : tail;
-    k_resolve_index<<<blocks_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(
-        P, tail, fb, rgba, rgba_words, image, clear_after, clear);
-    return launch_status();
+    return launch_k(k_resolve_index, blocks_for(threads, 256), 256, (cudaStream_t)stream, P, tail,
+                    fb, rgba, rgba_words, image, clear_after, clear);
 }
 
 int launch_resolve_color(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
                          uint64_t clear, void* stream) {
     int64_t P = (int64_t)W * H, tail = (int64_t)W + 1;
     int64_t threads = (P + 1) / 2 > tail ? (P + 1) / 2 : tail;
-    k_resolve_color<<<blocks_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(
-        P, tail, fb, image, clear_after, clear);
-    return launch_status();
+    return launch_k(k_resolve_color, blocks_for(threads, 256), 256, (cudaStream_t)stream, P, tail,
+                    fb, image, clear_after, clear);
 }
 
 int launch_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
-                         uint64_t clear, void* stream) {
+                         uint64_t clear, int tiles, int zero_rule, void* stream) {
     int64_t P = (int64_t)W * H, tail = (int64_t)W + 1;
     int64_t threads = P > tail ? P : tail;
-    k_resolve_plain<<<blocks_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(P, tail, fb, image,
-                                                                                 clear_after, clear);
-    return launch_status();
+    return launch_k(k_resolve_plain, blocks_for(threads, 256), 256, (cudaStream_t)stream, P, tail,
+                    W, H, tiles, zero_rule, fb, image, clear_after, clear);
 }
 
 int launch_resolve_hqs(int32_t W, int32_t H, uint32_t* depth, uint64_t* accum, uint32_t* image,
                        int clear_after, void* stream) {
     int64_t P = (int64_t)W * H, tail = (int64_t)W + 1;
     int64_t threads = P > tail ? P : tail;
-    k_resolve_hqs<<<blocks_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(P, tail, depth, accum,
-                                                                               image, clear_after);
-    return launch_status();
+    return launch_k(k_resolve_hqs, blocks_for(threads, 256), 256, (cudaStream_t)stream, P, tail,
+                    depth, accum, image, clear_after);
 }
 
 int launch_check_reciprocal(uint64_t* bad, uint32_t* first) {
     int device = 0, sms = 1;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    k_check_reciprocal<<<sms * 8, 256>>>(reinterpret_cast<unsigned long long*>(bad), first);
-    if (launch_status() != 0) return -1;
+    if (cudaGetDevice(&device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return -1;
+    if (launch_k(k_check_reciprocal, sms * 8, 256, (cudaStream_t)0,
+                 reinterpret_cast<unsigned long long*>(bad), first) != 0)
+        return -1;
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : -1;
 }
 
@@ -770,16 +832,14 @@ int launch_fill_u64(uint64_t* p, int64_t n, uint64_t v, void* stream) {
     if (n <= 0) return 0;
     int grid = blocks_for(n, 256);
     if (grid > 65535) grid = 65535;
-    k_fill_u64<<<grid, 256, 0, (cudaStream_t)stream>>>(p, n, v);
-    return launch_status();
+    return launch_k(k_fill_u64, grid, 256, (cudaStream_t)stream, p, n, v);
 }
 
 int launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, void* stream) {
     if (n <= 0) return 0;
     int grid = blocks_for(n, 256);
     if (grid > 65535) grid = 65535;
-    k_fill_u32<<<grid, 256, 0, (cudaStream_t)stream>>>(p, n, v);
-    return launch_status();
+    return launch_k(k_fill_u32, grid, 256, (cudaStream_t)stream, p, n, v);
 }
 
 }  // namespace cr

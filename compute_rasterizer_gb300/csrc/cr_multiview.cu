@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "cr_device.cuh"
+#include "cr_filerec.h"
 #include "cr_internal.h"
 
 namespace cr {
@@ -44,6 +45,37 @@ struct MVArgs {
 };
 
 constexpr int kSlotWords = 16;  // per view slot in shared memory: T[12], Wf, Hf, W, fb_off
+
+// The 12 transform entries of a view's T that the projection uses.
+__host__ __device__ inline void mv_file_from_rec(const FileRec& r, MVFile* o) {
+    const int pick[12] = {0, 1, 3, 4, 5, 7, 8, 9, 11, 12, 13, 15};
+    for (int k = 0; k < 12; k++) o->T[k] = r.T[pick[k]];
+    for (int k = 0; k < 24; k++) o->planes[k] = r.planes[k];
+    for (int k = 0; k < 16; k++) o->VW[k] = r.VW[k];
+}
+
+// Per (view, file) records of a frame for clouds with more than kInlineFiles
+// files (grid x: files, grid y strides over the views): the host's
+// file_record on the device, bit for bit (cr_filerec.h).
+__global__ void __launch_bounds__(128) k_mv_file_records(const double* __restrict__ mats,
+                                                         const double* __restrict__ box,
+                                                         int32_t nviews, int32_t nfiles,
+                                                         MVFile* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nfiles) return;
+    double bmin[3];
+    for (int k = 0; k < 3; k++) bmin[k] = box[3 * (int64_t)f + k];
+    for (int v = blockIdx.y; v < nviews; v += gridDim.y) {
+        double view[16], proj[16];
+        for (int k = 0; k < 16; k++) {
+            view[k] = mats[32 * (int64_t)v + k];
+            proj[k] = mats[32 * (int64_t)v + 16 + k];
+        }
+        FileRec r;
+        file_record(view, proj, bmin, &r);
+        mv_file_from_rec(r, &out[(int64_t)v * nfiles + f]);
+    }
+}
 
 __global__ void __launch_bounds__(256) k_mv_cull(const MVView* __restrict__ views,
                                                  const MVFile* __restrict__ files, int32_t nviews,
@@ -256,7 +288,11 @@ __device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
 
         const int64_t v0 = first >> 2;
         const int32_t head = (int32_t)(first & 3);
-        const int nv = (head + count + 3) >> 2;
+        // CR_QUIRK_UVEC4_BASE (las2/render.cs:319-341), as in the single-view
+        // raster: with firstPoint % 4 != 0 the vectors v % 128 == 0 (the
+        // reference's thread 0) are skipped and none past 2559 is read
+        const bool uvec4 = head != 0 && (a.quirks & CR_QUIRK_UVEC4_BASE) != 0;
+        const int nv = uvec4 ? min((head + count + 3) >> 2, kPointsPerBatch / 4) : (head + count + 3) >> 2;
         const uint32_t index0 = (uint32_t)(first - head);
         const uint4* lo4 = reinterpret_cast<const uint4*>(a.lo) + v0;
         const uint4* md4 = reinterpret_cast<const uint4*>(a.md) + v0;
@@ -285,6 +321,7 @@ __device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
 #pragma unroll
             for (int j = 0; j < 4; j++)
                 valid_mask |= ((uint32_t)(rel0 + j) < (uint32_t)count ? 1u : 0u) << j;
+            if (uvec4 && (v & 127) == 0) valid_mask = 0;
             const uint32_t idx0 = index0 + 4u * (uint32_t)v;
             Decoded d;
             if (LIST == 0) decode4(2, w4, w8, w12, mnx, mny, mnz, sc, l0_x12, d);
@@ -381,9 +418,7 @@ cudaError_t launch_mv_lists(const MVArgs& a, int grid, cudaStream_t s) {
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int grid1 = std::min(grid, sms * mv_occupancy_list1<PAYLOAD, BLOCK>());
-    k_mv_raster<PAYLOAD, BLOCK, 1><<<grid1, BLOCK, 0, s>>>(a);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (launch_k(k_mv_raster<PAYLOAD, BLOCK, 1>, grid1, BLOCK, s, a) != 0) return cudaErrorLaunchFailure;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(BLOCK);
@@ -437,14 +472,8 @@ cr_status mv_fill_view(const cr_view* view, const CloudInfo& ci, MVView* out_vie
     std::memcpy(out_view->P, vp.P, sizeof(vp.P));
     out_view->W = view->width;
     out_view->H = view->height;
-    const int pick[12] = {0, 1, 3, 4, 5, 7, 8, 9, 11, 12, 13, 15};
-    for (int f = 0; f < ci.nfiles; f++) {
-        MVFile& o = out_files[f];
-        const FileRec& r = vp.files[f];
-        for (int k = 0; k < 12; k++) o.T[k] = r.T[pick[k]];
-        std::memcpy(o.planes, r.planes, sizeof(o.planes));
-        std::memcpy(o.VW, r.VW, sizeof(o.VW));
-    }
+    if (ci.nfiles <= kInlineFiles)
+        for (int f = 0; f < ci.nfiles; f++) mv_file_from_rec(vp.files[f], &out_files[f]);
     return CR_OK;
 }
 
@@ -458,19 +487,26 @@ cr_status mv_enqueue(const MVFrame& f, void* stream, const char** what) {
     const int64_t words = std::max<int64_t>(f.max_words, 1);
     if (f.clear_before) {
         const unsigned gx = (unsigned)std::min<int64_t>((words + 255) / 256, 4096);
-        k_mv_fill_views<<<dim3(gx, (unsigned)f.nviews), 256, 0, st>>>(
-            f.d_views, reinterpret_cast<unsigned long long*>(f.fbs), f.clear_value);
-        if (cudaGetLastError() != cudaSuccess) return fail("fill launch");
+        if (launch_k(k_mv_fill_views, dim3(gx, (unsigned)f.nviews), 256, st, f.d_views,
+                     reinterpret_cast<unsigned long long*>(f.fbs), f.clear_value) != 0)
+            return fail("fill launch");
     }
     const int G = std::max(1, std::min(f.G, f.nviews));
     const int ngroups = (f.nviews + G - 1) / G;
     const int64_t nb = dispatched(f.ci, f.quirks);
     const int64_t threads = nb * ngroups;
+    if (f.ci.nfiles > kInlineFiles) {
+        if (!f.d_mats || !f.d_box) return fail("file records");
+        const unsigned gy = (unsigned)std::min(f.nviews, 65535);
+        if (launch_k(k_mv_file_records, dim3((unsigned)((f.ci.nfiles + 127) / 128), gy), 128, st,
+                     f.d_mats, f.d_box, f.nviews, f.ci.nfiles, const_cast<MVFile*>(f.d_files)) != 0)
+            return fail("file record launch");
+    }
     if (threads > 0) {
-        k_mv_cull<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-            f.d_views, f.d_files, f.nviews, f.ci.nfiles, G, ngroups, f.ci.batches, nb,
-            f.ci.capacity, f.quirks, f.culling, f.lod_skip_level, f.scratch);
-        if (cudaGetLastError() != cudaSuccess) return fail("cull launch");
+        if (launch_k(k_mv_cull, (unsigned)((threads + 255) / 256), 256, st, f.d_views, f.d_files,
+                     f.nviews, f.ci.nfiles, G, ngroups, f.ci.batches, nb, f.ci.capacity, f.quirks,
+                     f.culling, f.lod_skip_level, f.scratch) != 0)
+            return fail("cull launch");
         MVArgs a;
         a.views = f.d_views;
         a.files = f.d_files;
@@ -497,10 +533,10 @@ cr_status mv_enqueue(const MVFrame& f, void* stream, const char** what) {
     }
     if (f.resolve) {
         const unsigned gx = (unsigned)((words + 255) / 256);
-        k_mv_resolve<<<dim3(gx, (unsigned)f.nviews), 256, 0, st>>>(
-            f.d_views, reinterpret_cast<unsigned long long*>(f.fbs), f.images, f.ci.rgba,
-            f.ci.capacity, f.payload, f.clear_after, f.clear_value);
-        if (cudaGetLastError() != cudaSuccess) return fail("resolve launch");
+        if (launch_k(k_mv_resolve, dim3(gx, (unsigned)f.nviews), 256, st, f.d_views,
+                     reinterpret_cast<unsigned long long*>(f.fbs), f.images, f.ci.rgba, f.ci.capacity,
+                     f.payload, f.clear_after, f.clear_value) != 0)
+            return fail("resolve launch");
     }
     return CR_OK;
 }
@@ -523,7 +559,11 @@ struct cr_mv {
     MVView* d_views = nullptr;
     MVFile* d_files = nullptr;
     MVView* h_views = nullptr;  // pinned staging
-    MVFile* h_files = nullptr;
+    MVFile* h_files = nullptr;  // clouds of at most kInlineFiles files
+    double* h_mats = nullptr;   // clouds with more files: view + proj per view,
+    double* d_mats = nullptr;   // and every file's boxMin, from which each frame
+    double* h_box = nullptr;    // computes d_files on the GPU
+    double* d_box = nullptr;
     uint32_t* scratch = nullptr;
     int num_sms = 0;
     cr_render_params params{};
@@ -579,11 +619,18 @@ cr_status apply_params(cr_mv* mv, const cr_render_params* p) {
 
 cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
     const cr_render_params& p = mv->params;
+    const bool many = mv->ci.nfiles > kInlineFiles;
     cudaError_t e = cudaMemcpyAsync(mv->d_views, mv->h_views, sizeof(MVView) * mv->nviews,
                                     cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !many)
         e = cudaMemcpyAsync(mv->d_files, mv->h_files,
                             sizeof(MVFile) * (size_t)mv->nviews * mv->ci.nfiles,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && many)
+        e = cudaMemcpyAsync(mv->d_mats, mv->h_mats, sizeof(double) * 32 * (size_t)mv->nviews,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && many)
+        e = cudaMemcpyAsync(mv->d_box, mv->h_box, sizeof(double) * 3 * (size_t)mv->ci.nfiles,
                             cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return mv_cuda(mv, e, "frame setup");
     MVFrame f{};
@@ -607,9 +654,11 @@ cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
     f.clear_after = p.clear_after;
     f.clear_value = p.clear_value;
     f.max_words = mv->max_words;
+    f.d_mats = mv->d_mats;
+    f.d_box = mv->d_box;
     const char* what = "";
     const cr_status s = mv_enqueue(f, st, &what);
-    if (s != CR_OK) return mv_cuda(mv, cudaGetLastError(), what);
+    if (s != CR_OK) return mv_fail(mv, s, std::string(what) + " failed");
     return CR_OK;
 }
 
@@ -626,7 +675,7 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
     if (!mv) return CR_ERR_OUT_OF_MEMORY;
     mv->ctx = ctx;
     mv->cloud = cloud;
-    if (!cloud_info(cloud, &mv->ci) || !mv->ci.md || !mv->ci.hi || mv->ci.nfiles > kInlineFiles) {
+    if (!cloud_info(cloud, &mv->ci) || !mv->ci.md || !mv->ci.hi) {
         delete mv;
         return CR_ERR_INVALID_ARG;
     }
@@ -666,8 +715,18 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
     if (e == cudaSuccess) e = cudaMalloc(&mv->scratch, mv_scratch_words(mv->ci.nb_total, nviews) * 4);
     if (e == cudaSuccess) e = cudaMemset(mv->scratch, 0, mv_scratch_words(mv->ci.nb_total, nviews) * 4);
     if (e == cudaSuccess) e = cudaHostAlloc(&mv->h_views, sizeof(MVView) * nviews, cudaHostAllocDefault);
-    if (e == cudaSuccess)
-        e = cudaHostAlloc(&mv->h_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles, cudaHostAllocDefault);
+    if (mv->ci.nfiles <= kInlineFiles) {
+        if (e == cudaSuccess)
+            e = cudaHostAlloc(&mv->h_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles,
+                              cudaHostAllocDefault);
+    } else {
+        if (e == cudaSuccess) e = cudaMalloc(&mv->d_mats, sizeof(double) * 32 * (size_t)nviews);
+        if (e == cudaSuccess) e = cudaMalloc(&mv->d_box, sizeof(double) * 3 * (size_t)mv->ci.nfiles);
+        if (e == cudaSuccess)
+            e = cudaHostAlloc(&mv->h_mats, sizeof(double) * 32 * (size_t)nviews, cudaHostAllocDefault);
+        if (e == cudaSuccess)
+            e = cudaHostAlloc(&mv->h_box, sizeof(double) * 3 * (size_t)mv->ci.nfiles, cudaHostAllocDefault);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&mv->done, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cr_mv_destroy(mv);
@@ -687,11 +746,12 @@ cr_status cr_mv_destroy(cr_mv* mv) {
     if (!mv) return CR_ERR_INVALID_ARG;
     if (mv->pending) cudaEventSynchronize(mv->done);
     drop_graph(mv);
-    void* dev[6] = {mv->fbs, mv->images, mv->d_views, mv->d_files, mv->scratch, nullptr};
+    void* dev[7] = {mv->fbs, mv->images, mv->d_views, mv->d_files, mv->scratch, mv->d_mats, mv->d_box};
     for (void* p : dev)
         if (p) cudaFree(p);
-    if (mv->h_views) cudaFreeHost(mv->h_views);
-    if (mv->h_files) cudaFreeHost(mv->h_files);
+    void* host[4] = {mv->h_views, mv->h_files, mv->h_mats, mv->h_box};
+    for (void* p : host)
+        if (p) cudaFreeHost(p);
     if (mv->done) cudaEventDestroy(mv->done);
     delete mv;
     return CR_OK;
@@ -723,10 +783,17 @@ cr_status cr_mv_set_views(cr_mv* mv, const cr_view* views) {
     for (int v = 0; v < mv->nviews; v++) {
         if (views[v].width != mv->W[v] || views[v].height != mv->H[v])
             return mv_fail(mv, CR_ERR_INVALID_ARG, "view " + std::to_string(v) + " size differs from the plan");
+        const bool many = mv->ci.nfiles > kInlineFiles;
         cr_status s = mv_fill_view(&views[v], mv->ci, &mv->h_views[v],
-                                   &mv->h_files[(int64_t)v * mv->ci.nfiles]);
+                                   many ? nullptr : &mv->h_files[(int64_t)v * mv->ci.nfiles]);
         if (s != CR_OK) return mv_fail(mv, s, "view " + std::to_string(v) + ": bad matrices");
+        if (many) {
+            std::memcpy(&mv->h_mats[32 * (int64_t)v], views[v].view, sizeof(double) * 16);
+            std::memcpy(&mv->h_mats[32 * (int64_t)v + 16], views[v].proj, sizeof(double) * 16);
+        }
     }
+    // the files' boxMin as the frames of these views read them
+    if (mv->h_box) std::memcpy(mv->h_box, mv->ci.box_min, sizeof(double) * 3 * (size_t)mv->ci.nfiles);
     mv->views_set = true;
     return CR_OK;
 }
@@ -778,8 +845,9 @@ cr_status cr_mv_clear(cr_mv* mv, uint64_t value, void* stream) {
     if (!mv) return CR_ERR_INVALID_ARG;
     const int64_t n = mv->total_words;
     const int grid = (int)std::min<int64_t>((n + 255) / 256, 65535);
-    k_mv_fill<<<grid, 256, 0, (cudaStream_t)stream>>>(mv->fbs, n, value);
-    return mv_cuda(mv, cudaGetLastError(), "clear launch");
+    if (launch_k(k_mv_fill, grid, 256, (cudaStream_t)stream, mv->fbs, n, value) != 0)
+        return mv_fail(mv, CR_ERR_CUDA, "clear launch failed");
+    return CR_OK;
 }
 
 cr_status cr_mv_read(cr_mv* mv, int32_t view, int32_t what, void* dst, int64_t bytes, void* stream) {

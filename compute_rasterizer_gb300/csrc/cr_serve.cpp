@@ -93,7 +93,8 @@ struct Pending {
     int64_t fb_bytes = 0, bytes = 0;  // chunk: [fb words, rounded][image]
     double t_arrival = 0.0;
     MVView view{};
-    MVFile files[cr::kInlineFiles];
+    MVFile files[cr::kInlineFiles];  // clouds of at most kInlineFiles files; with
+                                     // more, the GPU computes them from r.view
 };
 
 struct Slot {
@@ -106,6 +107,17 @@ struct Slot {
     MVView* h_views = nullptr;  // pinned
     MVFile* h_files = nullptr;  // pinned
     uint32_t* h_err = nullptr;  // pinned copy of the device error word
+    // clouds with more than kInlineFiles files: view + proj per request
+    // (pinned and device), every file's boxMin (pinned and device), the
+    // multi-view records (d_files, files_cap per view) and the single-view
+    // records (d_frec), grown to the largest file count launched
+    double* h_mats = nullptr;
+    double* d_mats = nullptr;
+    double* h_box = nullptr;
+    double* d_box = nullptr;
+    cr::FileRec* d_frec = nullptr;
+    int32_t files_cap = cr::kInlineFiles;  // files per view d_files / h_files hold
+    int32_t many_cap = 0;                  // files h_box, d_box and d_frec hold
     bool busy = false;
     std::vector<Pending> reqs;
     std::vector<int64_t> offs;
@@ -227,6 +239,33 @@ cudaError_t ensure_slot_scratch(Slot& sl, int64_t words) {
     return e;
 }
 
+// Grows a free slot's per-file buffers to `nfiles` files (its stream is idle).
+cudaError_t ensure_slot_files(Slot& sl, int32_t nfiles, int maxv) {
+    cudaError_t e = cudaSuccess;
+    if (nfiles > sl.files_cap) {
+        if (sl.d_files) cudaFree(sl.d_files);
+        sl.d_files = nullptr;
+        e = cudaMalloc(&sl.d_files, sizeof(MVFile) * (size_t)maxv * nfiles);
+        if (e != cudaSuccess) return e;
+        sl.files_cap = nfiles;
+    }
+    if (nfiles > cr::kInlineFiles && nfiles > sl.many_cap) {
+        if (sl.h_box) cudaFreeHost(sl.h_box);
+        if (sl.d_box) cudaFree(sl.d_box);
+        if (sl.d_frec) cudaFree(sl.d_frec);
+        sl.h_box = nullptr;
+        sl.d_box = nullptr;
+        sl.d_frec = nullptr;
+        sl.many_cap = 0;
+        e = cudaHostAlloc(&sl.h_box, sizeof(double) * 3 * (size_t)nfiles, cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_box, sizeof(double) * 3 * (size_t)nfiles);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_frec, sizeof(cr::FileRec) * (size_t)nfiles);
+        if (e != cudaSuccess) return e;
+        sl.many_cap = nfiles;
+    }
+    return cudaSuccess;
+}
+
 // Enqueues the frame of the requests in sl.reqs (chunks at sl.offs).
 cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what) {
     const cr_server_config& c = s->cfg;
@@ -241,6 +280,8 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
     }
     cudaError_t e = injected > 0 ? cudaErrorMemoryAllocation
                                  : ensure_slot_scratch(sl, cr::mv_scratch_words(nb, single ? 1 : n));
+    if (e == cudaSuccess)
+        e = ensure_slot_files(sl, ci.nfiles, c.plain_launches ? 1 : c.max_batch_views);
     if (e != cudaSuccess) {
         *what = "scratch allocation";
         return CR_ERR_OUT_OF_MEMORY;
@@ -263,6 +304,14 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
                 *what = "view matrices";
                 return CR_ERR_INVALID_ARG;
             }
+            if (ci.nfiles > cr::kInlineFiles) {
+                if (cr::launch_file_records(p.r.view.view, p.r.view.proj, ci.box_min, ci.nfiles,
+                                            sl.d_frec, sl.st) != 0) {
+                    *what = "file record launch";
+                    return CR_ERR_CUDA;
+                }
+                vp.dfiles = sl.d_frec;
+            }
             if (cr::launch_fill_u64(fb, (int64_t)W * H + W + 1, cr::kDefaultClear, sl.st) != 0 ||
                 cudaMemsetAsync(sl.scratch, 0, cr::kCounterWords * 4, sl.st) != cudaSuccess ||
                 cr::launch_cull(vp, ci.batches, nb, ci.capacity, s->quirks, sl.scratch, sl.st) != 0) {
@@ -283,7 +332,8 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
             bl.payload = c.payload;
             bl.mode = cr::kModeRaster;
             const int block = c.plain_launches && c.block_threads > 0 ? c.block_threads : 128;
-            const int per_sm = std::max(1, cr::batched_blocks_per_sm(bl.mode, bl.payload, block));
+            const int per_sm = std::max(
+                1, cr::batched_blocks_per_sm(bl.mode, bl.payload, block, ci.nfiles > cr::kInlineFiles));
             if (cr::launch_batched(vp, bl, block, s->num_sms * per_sm, sl.st) != 0) {
                 *what = "plain raster launch";
                 return CR_ERR_CUDA;
@@ -298,20 +348,34 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
             }
         }
     } else {
+        const bool many = ci.nfiles > cr::kInlineFiles;
         int64_t max_words = 1;
         for (int i = 0; i < n; i++) {
             const Pending& p = sl.reqs[i];
             sl.h_views[i] = p.view;
             sl.h_views[i].fb_off = (uint32_t)(sl.offs[i] / 8);
             sl.h_views[i].img_off = (uint32_t)((sl.offs[i] + p.fb_bytes) / 4);
-            std::memcpy(&sl.h_files[(int64_t)i * ci.nfiles], p.files, sizeof(MVFile) * ci.nfiles);
+            if (many) {
+                std::memcpy(&sl.h_mats[32 * (int64_t)i], p.r.view.view, sizeof(double) * 16);
+                std::memcpy(&sl.h_mats[32 * (int64_t)i + 16], p.r.view.proj, sizeof(double) * 16);
+            } else {
+                std::memcpy(&sl.h_files[(int64_t)i * ci.nfiles], p.files, sizeof(MVFile) * ci.nfiles);
+            }
             const int64_t W = p.r.view.width, H = p.r.view.height;
             max_words = std::max(max_words, W * H + W + 1);
         }
         e = cudaMemcpyAsync(sl.d_views, sl.h_views, sizeof(MVView) * n, cudaMemcpyHostToDevice, sl.st);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess && !many)
             e = cudaMemcpyAsync(sl.d_files, sl.h_files, sizeof(MVFile) * (size_t)n * ci.nfiles,
                                 cudaMemcpyHostToDevice, sl.st);
+        if (e == cudaSuccess && many) {
+            std::memcpy(sl.h_box, ci.box_min, sizeof(double) * 3 * (size_t)ci.nfiles);
+            e = cudaMemcpyAsync(sl.d_mats, sl.h_mats, sizeof(double) * 32 * (size_t)n,
+                                cudaMemcpyHostToDevice, sl.st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(sl.d_box, sl.h_box, sizeof(double) * 3 * (size_t)ci.nfiles,
+                                    cudaMemcpyHostToDevice, sl.st);
+        }
         if (e != cudaSuccess) {
             *what = "view upload";
             return CR_ERR_CUDA;
@@ -336,6 +400,8 @@ cr_status enqueue(cr_server* s, Slot& sl, const CloudInfo& ci, const char** what
         f.resolve = 1;
         f.clear_after = 0;
         f.max_words = max_words;
+        f.d_mats = sl.d_mats;
+        f.d_box = sl.d_box;
         const cr_status st = cr::mv_enqueue(f, sl.st, what);
         if (st != CR_OK) return st;
     }
@@ -477,6 +543,11 @@ void free_server(cr_server* s) {
         if (sl.h_views) cudaFreeHost(sl.h_views);
         if (sl.h_files) cudaFreeHost(sl.h_files);
         if (sl.h_err) cudaFreeHost(sl.h_err);
+        if (sl.h_mats) cudaFreeHost(sl.h_mats);
+        if (sl.d_mats) cudaFree(sl.d_mats);
+        if (sl.h_box) cudaFreeHost(sl.h_box);
+        if (sl.d_box) cudaFree(sl.d_box);
+        if (sl.d_frec) cudaFree(sl.d_frec);
         if (sl.ev0) cudaEventDestroy(sl.ev0);
         if (sl.ev1) cudaEventDestroy(sl.ev1);
         if (sl.st) cudaStreamDestroy(sl.st);
@@ -540,6 +611,8 @@ cr_status cr_server_create(cr_ctx* ctx, const cr_server_config* cfg, cr_server**
             e = cudaHostAlloc(&sl.h_files, sizeof(MVFile) * maxv * cr::kInlineFiles, cudaHostAllocDefault);
         if (e == cudaSuccess) e = cudaHostAlloc(&sl.h_err, 4, cudaHostAllocDefault);
         if (e == cudaSuccess) *sl.h_err = 0;
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_mats, sizeof(double) * 32 * maxv);
+        if (e == cudaSuccess) e = cudaHostAlloc(&sl.h_mats, sizeof(double) * 32 * maxv, cudaHostAllocDefault);
     }
     if (e != cudaSuccess) {
         const cr_status st = e == cudaErrorMemoryAllocation ? CR_ERR_OUT_OF_MEMORY : CR_ERR_CUDA;
@@ -575,7 +648,7 @@ double cr_server_now_us(const cr_server* s) { return s ? now_us(s) : 0.0; }
 cr_status cr_server_add_cloud(cr_server* s, const cr_cloud* cloud, int32_t* id) {
     if (!s || !cloud || !id) return CR_ERR_INVALID_ARG;
     CloudInfo ci;
-    if (!cr::cloud_info(cloud, &ci) || !ci.md || !ci.hi || !ci.rgba || ci.nfiles > cr::kInlineFiles)
+    if (!cr::cloud_info(cloud, &ci) || !ci.md || !ci.hi || !ci.rgba)
         return set_err(s, CR_ERR_INVALID_ARG, "the server renders LAS-derived clouds with all four streams");
     std::lock_guard<std::mutex> lk(s->cloud_mu);
     *id = (int32_t)s->clouds.size();

@@ -30,9 +30,15 @@
 extern "C" {
 #endif
 
-#define CR_ABI_VERSION 1
+#define CR_ABI_VERSION 2
 #define CR_POINTS_PER_BATCH 10240 /* Resources.h:4-6: POINTS_PER_THREAD 80 x WORKGROUP_SIZE 128 */
 #define CR_MAX_POINTS_PER_LOAD 1024000 /* Resources.h:8 MAX_POINTS_PER_BATCH */
+/* Files per cloud: each batch record names its file (`fileIndex`), whose
+ * boxMin places it in the world (render.cs:44-49; the reference's file SSBO
+ * holds 5,000 records, compute_loop_las.h:100).  The first 8 files' per-view
+ * uniforms travel in kernel parameters; with more files every file's record
+ * is computed on the GPU into device memory each frame. */
+#define CR_MAX_FILES 65536
 
 typedef enum cr_status {
     CR_OK = 0,
@@ -66,9 +72,18 @@ typedef enum cr_payload {
 /* Reference behaviours kept for drop-in parity (each method's default set is
  * what the reference does; pass 0 for the corrected behaviour). */
 typedef enum cr_quirk {
-    CR_QUIRK_L0_X12 = 1,            /* 30-bit decode takes Y, Z low bits from X (render.cs:352-353) */
-    CR_QUIRK_INCLUSIVE_END = 2,     /* `localIndex > numPoints` (las2/render.cs:341, hqs/depth.cs:276) */
-    CR_QUIRK_DISPATCH_BY_POINTS = 4 /* ceil(numPoints/10240) workgroups (compute_loop_las2.h:234) */
+    CR_QUIRK_L0_X12 = 1,             /* 30-bit decode takes Y, Z low bits from X (render.cs:352-353) */
+    CR_QUIRK_INCLUSIVE_END = 2,      /* `localIndex > numPoints` (las2/render.cs:341, hqs/depth.cs:276) */
+    CR_QUIRK_DISPATCH_BY_POINTS = 4, /* ceil(numPoints/10240) workgroups (compute_loop_las2.h:234) */
+    /* loop_las_prefetch's uvec4 addressing from firstPoint/4 (las2/render.cs:319-341): when
+     * firstPoint % 4 = r != 0, thread 0 underflows localIndex and returns, so the batch points
+     * l with (l + r) % 512 < 4 are skipped, and the last r points (l >= 10240 - r) are never
+     * visited.  Batched single-view, multi-view and server paths. */
+    CR_QUIRK_UVEC4_BASE = 8,
+    /* The 2021 methods' resolve dispatches floor(W/16) x floor(H/16) groups of 16x16
+     * (compute_2021_earlyz.h:161-163): pixels outside those tiles are neither resolved nor
+     * re-cleared; their image and framebuffer words keep their values. */
+    CR_QUIRK_PLAIN_TILES = 16
 } cr_quirk;
 
 #define CR_QUIRKS_METHOD_DEFAULT (-1)
@@ -133,7 +148,8 @@ cr_status cr_ctx_create(int32_t device, cr_ctx** out);
 cr_status cr_ctx_destroy(cr_ctx* ctx);
 const char* cr_last_error(const cr_ctx* ctx);
 /* Waits for `stream`, then reports a device-side error flag raised since the
- * last check (CR_ERR_DEVICE_FLAG) and clears it. */
+ * last check (CR_ERR_DEVICE_FLAG) and clears it.  ctx = NULL checks the flag
+ * of cr_render_batched_noalloc's fixed array in the current CUDA context. */
 cr_status cr_ctx_check(cr_ctx* ctx, void* stream);
 /* Self-check of the kernels' reciprocal (the correctly rounded 1/w that every
  * `xy / w` uses, render.cs:402): runs it against CUDA's __frcp_rn over all 2^32
@@ -147,7 +163,8 @@ enum { CR_STREAM_LOW = 1, CR_STREAM_MED = 2, CR_STREAM_HIG = 4, CR_STREAM_RGBA =
 
 /* Allocates device storage for `num_points` points in `num_batches` records
  * across `num_files` files (per-file boxMin feeds the world matrix).
- * num_points < 2^31 - 64 and num_batches < 2^28 (cr_cloud_wrap alike). */
+ * num_points < 2^31 - 64, num_batches < 2^28 and 1 <= num_files <=
+ * CR_MAX_FILES (cr_cloud_wrap alike). */
 cr_status cr_cloud_create(cr_ctx* ctx, int64_t num_points, int64_t num_batches, int32_t num_files,
                           int32_t stream_mask, cr_cloud** out);
 /* Host -> device copies (pinned or pageable).  Any stream pointer may be NULL
@@ -278,25 +295,38 @@ cr_status cr_mv_autotune(cr_mv* mv, int32_t frames, void* stream, cr_render_para
 /* ---- rasterizing without allocating ------------------------------------------
  * No counterpart in the reference (its Methods own GL buffers created at
  * start-up).  For callers that must not allocate device memory while they
- * render: a host engine that owns the GPU memory budget, a plugin running
- * inside someone else's frame loop, or code that records work into a CUDA
- * graph, where cudaMalloc/cudaFree synchronise the device or are not allowed.
- * Same cull + raster as cr_render for the batched methods (loop_las,
- * loop_las_prefetch; no resolve, no HQS) on caller-owned device buffers; its
- * work list lives in a fixed device array inside the library, sized for at
- * most CR_NOALLOC_MAX_BATCHES batch records (512 KB, held on every GPU that
- * loads the library until the process exits).  It allocates nothing: no
+ * render: a host engine that owns the GPU memory budget and hands the renderer
+ * only buffers it already placed, or a plugin running inside someone else's
+ * frame loop, where a cudaMalloc or cudaFree would synchronise the device or
+ * disturb the host application's own work.  Same cull + raster as cr_render
+ * for the batched methods (loop_las, loop_las_prefetch; no resolve, no HQS)
+ * on caller-owned device buffers.  Its work list and, for clouds with more
+ * than 8 files, the per-file records live in one fixed device array inside
+ * the library (CR_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the
+ * library until the process exits), sized for at most CR_NOALLOC_MAX_BATCHES
+ * batch records and CR_NOALLOC_MAX_FILES files.  It allocates nothing: no
  * cudaMalloc, cudaFree or allocating library call.
  *   - `fb` holds width*height + width + 1 words, already cleared by the caller.
  *   - streams hold `stream_words` words each, with at least 64 zeroed words
  *     past the last point (the padding cr_cloud_create adds).
- *   - The first call on a device looks up the array's device address (once per
- *     device, with that device current); make that first call before any
+ *   - `file_box_min` is a host array of 3 * num_files doubles.
+ *   - params->resolve and params->clear_after must be 0.
+ *   - The first call in each CUDA context (the device's primary context, or
+ *     one the caller made with cuCtxCreate and made current) looks up the
+ *     array's device address in that context; make that first call before any
  *     stream capture.
- *   - Every call shares the one array, so calls whose work overlaps on the GPU
- *     (other streams, other threads) race; serialise them on one stream.
- * Returns CR_ERR_INVALID_ARG past the size limit or for bad arguments. */
+ *   - Every call shares the one array, which keeps the previous call's
+ *     contents (each call resets what must start at zero), so calls whose work
+ *     overlaps on the GPU (other streams, other threads) race; serialise them
+ *     on one stream.
+ *   - A batch record out of range (num_points, first_point + num_points past
+ *     stream_words, file_index >= num_files) is skipped without a fault and
+ *     sets the array's error flag, which cr_ctx_check(NULL, stream) reports
+ *     (CR_ERR_DEVICE_FLAG) and clears.
+ * Returns CR_ERR_INVALID_ARG past the size limits or for bad arguments. */
 #define CR_NOALLOC_MAX_BATCHES 131064
+#define CR_NOALLOC_MAX_FILES 1024
+#define CR_NOALLOC_SCRATCH_BYTES 753664 /* (8 + 131064) * 4 + 1024 * 224 */
 cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_t num_batches,
                                     int64_t num_points, const uint32_t* d_xyz_low,
                                     const uint32_t* d_xyz_med, const uint32_t* d_xyz_hig,
@@ -304,6 +334,10 @@ cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_t num_batch
                                     const double* file_box_min, int32_t num_files,
                                     const cr_view* view, const cr_render_params* params,
                                     uint64_t* d_fb, void* stream);
+/* The fixed array's device address in the calling thread's current CUDA
+ * context (looked up there on first use, as by the render call) and its size
+ * in bytes, for callers that account for device memory. */
+cr_status cr_noalloc_scratch(void** device_address, int64_t* bytes);
 
 /* ---- timer queries and frame counters --------------------------------------
  * GLTimerQueries::timestamp pairs (src/GLTimerQueries.cpp:6-22) around the

@@ -381,7 +381,15 @@ static void raster_range(const raster_job* j) {
         batch_decode d;
         make_decode(b, level, &d);
         int64_t count = or_points_in_batch(b, fr->quirks);
+        /* H6, compute_loop_las2/render.cs:319-341: base = firstPoint / 4 + tid; thread
+         * t's point (i, j) is index 4 * (base + 128 i) + j, i.e. batch point
+         * l = 4 t + 512 i + j - r with r = firstPoint % 4.  Thread 0's first
+         * localIndex (j - r) underflows the uint compare, so thread 0 returns at
+         * once and every l with (l + r) % 512 < 4 is skipped; the threads reach
+         * l = 10239 - r at most, so the last r points are never visited. */
+        const int32_t r = (fr->quirks & OR_QUIRK_UVEC4_BASE) ? (b->first_point & 3) : 0;
         for (int64_t l = 0; l < count; l++) {
+            if (r != 0 && (l >= POINTS_PER_BATCH - r || ((l + r) & 511) < 4)) continue;
             int64_t idx = (int64_t)b->first_point + l;
             float p[3], w;
             int32_t pix;
@@ -623,22 +631,35 @@ void or_raster_plain_warp(const float T[16], int32_t W, int32_t H, const or_vert
 
 /* compute_2021_earlyz/resolve.cs:41-77: 24-bit color to RGBA8 through
  * unpackUnorm4x8 (c / 255) * 255, color 0 -> opaque black; then re-clear. */
-void or_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint8_t* out, uint64_t reclear) {
-    int64_t P = (int64_t)W * H;
-    for (int64_t p = 0; p < P; p++) {
-        uint32_t ucol = (uint32_t)(fb[p] & 0x00FFFFFFu);
-        uint8_t* o = out + 4 * p;
-        if (ucol == 0) {
-            o[0] = 0; o[1] = 0; o[2] = 0; o[3] = 255;
-        } else {
-            for (int k = 0; k < 4; k++) {
-                float c = (float)((ucol >> (8 * k)) & 0xFFu);
-                float f = 255.0f * (c / 255.0f);
-                o[k] = (uint8_t)(uint32_t)f;
+/* compute_2021_earlyz/resolve.cs:41-77, compute_2021_dedup/resolve.cs:15-42,
+ * compute_2021_earlyz_reduce/resolve.cs:41-77.  The reference dispatches
+ * floor(W/16) x floor(H/16) groups of 16 x 16 threads (compute_2021_earlyz.h:
+ * 161-163), so with OR_QUIRK_PLAIN_TILES the pixels past the last full tile
+ * keep their image and framebuffer words.  Without it every pixel is resolved
+ * and the framebuffer's guard tail (W + 1 words past W*H) is re-cleared too. */
+void or_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint8_t* out, uint64_t reclear,
+                      int32_t quirks, int32_t zero_rule) {
+    const int tiles = (quirks & OR_QUIRK_PLAIN_TILES) != 0;
+    const int32_t Wt = tiles ? W / 16 * 16 : W, Ht = tiles ? H / 16 * 16 : H;
+    for (int32_t y = 0; y < Ht; y++) {
+        for (int32_t x = 0; x < Wt; x++) {
+            const int64_t p = (int64_t)x + (int64_t)y * W;
+            uint32_t ucol = (uint32_t)(fb[p] & 0x00FFFFFFu);
+            uint8_t* o = out + 4 * p;
+            if (ucol == 0 && zero_rule) {
+                o[0] = 0; o[1] = 0; o[2] = 0; o[3] = 255;
+            } else {
+                for (int k = 0; k < 4; k++) {
+                    float c = (float)((ucol >> (8 * k)) & 0xFFu);
+                    float f = 255.0f * (c / 255.0f);
+                    o[k] = (uint8_t)(uint32_t)f;
+                }
             }
+            fb[p] = reclear;
         }
-        fb[p] = reclear;
     }
+    if (!tiles)
+        for (int64_t t = 0; t <= W; t++) fb[(int64_t)W * H + t] = reclear;
 }
 
 /* ------------------------------------------------------------------------- */

@@ -73,7 +73,9 @@ typedef struct or_file_frame {
 enum {
     OR_QUIRK_L0_X12 = 1,       /* H1: 30-bit decode uses X_12 for Y and Z (render.cs:352-353) */
     OR_QUIRK_INCLUSIVE_END = 2, /* H2: `localIndex > numPoints` bound (las2/render.cs:341, hqs/depth.cs:276) */
-    OR_QUIRK_DISPATCH_BY_POINTS = 4 /* H3: dispatch ceil(numPoints/10240) batch records (compute_loop_las2.h:234) */
+    OR_QUIRK_DISPATCH_BY_POINTS = 4, /* H3: dispatch ceil(numPoints/10240) batch records (compute_loop_las2.h:234) */
+    OR_QUIRK_UVEC4_BASE = 8,  /* H6: las2's uvec4 addressing from firstPoint/4 (las2/render.cs:319-341) */
+    OR_QUIRK_PLAIN_TILES = 16 /* the 2021 resolves cover floor(W/16) x floor(H/16) tiles (compute_2021_earlyz.h:161-163) */
 };
 
 enum { OR_PAYLOAD_INDEX = 0, OR_PAYLOAD_COLOR = 1 };
@@ -142,8 +144,10 @@ void or_raster_plain(const float transform[16], int32_t width, int32_t height,
  * warp reductions over 32 consecutive points, key depth << 24 | color. */
 void or_raster_plain_warp(const float T[16], int32_t W, int32_t H, const or_vertex* v, int64_t n,
                           uint64_t* fb, int32_t variant);
+/* quirks: OR_QUIRK_PLAIN_TILES; zero_rule: ucol == 0 resolves to (0,0,0,255)
+ * (early-z and early-z & reduce; the dedup resolve has no such rule). */
 void or_resolve_plain(int32_t width, int32_t height, uint64_t* fb, uint8_t* out_rgba8,
-                      uint64_t reclear);
+                      uint64_t reclear, int32_t quirks, int32_t zero_rule);
 
 /* ---- LAS-derived layout builder: LasLoaderSparse.cpp:37-212 (A1, A2) ----- */
 int64_t or_num_batches(int64_t n);

@@ -15,7 +15,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 GLMREF = HERE / "_ref" / "libglmref.so"
 
-L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS = 1, 2, 4
+L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS, UVEC4_BASE, PLAIN_TILES = 1, 2, 4, 8, 16
 PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
 
 
@@ -31,8 +31,19 @@ class Frame(C.Structure):
                 ("files", C.POINTER(FileFrame))]
 
 
+# Where the reference checkout is read from to build the glm probe: the
+# CR_REFERENCE environment variable, else the checkout this build reads from.
+REFERENCE_CHECKOUT = "/root/reference"
+
+
+def reference_dir() -> str:
+    import os
+    ref = os.environ.get("CR_REFERENCE") or REFERENCE_CHECKOUT
+    return ref if Path(ref, "libs", "glm", "glm").is_dir() else ""
+
+
 def build() -> None:
-    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), f"REF={reference_dir()}"], check=True)
 
 
 _lib = None
@@ -58,7 +69,7 @@ def lib() -> C.CDLL:
             "or_plain_transform": [P, P, P],
             "or_raster_plain": [P, I32, I32, P, I64, P],
             "or_raster_plain_warp": [P, I32, I32, P, I64, P, I32],
-            "or_resolve_plain": [I32, I32, P, P, C.c_uint64],
+            "or_resolve_plain": [I32, I32, P, P, C.c_uint64, I32, I32],
             "or_encode_las": [P, I64, I32, I32, P, P, P, I64, I32, P, P, P, P, P],
             "or_encode_standard": [P, I64, I32, I32, P, P, P, P],
             "or_precision_level": [C.POINTER(Frame), C.POINTER(FileFrame), P, P],
@@ -184,21 +195,28 @@ def hqs(frame, batches, n, low, med, hig, rgba):
 
 
 def plain(view, proj, width, height, vertices, clear=0xFFFFFFFFFFFFFFFF,
-          reclear=0xFFFFFFFFFF3C321E, variant=0):
-    """The plain 16 B path: variant 0 early-z, 1 dedup, 2 early-z & reduce."""
+          reclear=0xFFFFFFFFFF3C321E, variant=0, quirks=PLAIN_TILES, fb=None, image=None):
+    """The plain 16 B path: variant 0 early-z, 1 dedup, 2 early-z & reduce.
+    quirks: PLAIN_TILES (the methods' default) or 0.  `fb` / `image`: the
+    previous frame's framebuffer and image (pixels outside the resolved tiles
+    keep them); a fresh fb filled with `clear` and a zero image by default.
+    Returns (fb after the raster, image, fb after the resolve)."""
     T = np.empty(16, np.float32)
     view = np.ascontiguousarray(view, np.float64).reshape(16)
     proj = np.ascontiguousarray(proj, np.float64).reshape(16)
     lib().or_plain_transform(_p(view), _p(proj), _p(T))
-    fb = np.full(fb_words(width, height), clear, dtype=np.uint64)
+    fb = (np.full(fb_words(width, height), clear, dtype=np.uint64) if fb is None
+          else np.array(fb, dtype=np.uint64))
     v = np.ascontiguousarray(vertices)
     if variant == 0:
         lib().or_raster_plain(_p(T), width, height, _p(v), len(v), _p(fb))
     else:
         lib().or_raster_plain_warp(_p(T), width, height, _p(v), len(v), _p(fb), int(variant))
     fb_before = fb.copy()
-    img = np.empty(width * height, dtype=np.uint32)
-    lib().or_resolve_plain(width, height, _p(fb), _p(img), reclear)
+    img = (np.zeros(width * height, dtype=np.uint32) if image is None
+           else np.array(image, dtype=np.uint32))
+    lib().or_resolve_plain(width, height, _p(fb), _p(img), reclear, int(quirks),
+                           0 if variant == 1 else 1)
     return fb_before, img, fb
 
 

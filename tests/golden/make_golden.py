@@ -27,7 +27,8 @@ from oracle import oracle as O  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "golden.json"
 
-QUIRKS = {"loop_las": O.L0_X12, "loop_las_prefetch": O.INCLUSIVE_END | O.DISPATCH_BY_POINTS,
+QUIRKS = {"loop_las": O.L0_X12,
+          "loop_las_prefetch": O.INCLUSIVE_END | O.DISPATCH_BY_POINTS | O.UVEC4_BASE,
           "loop_las_hqs": O.L0_X12 | O.INCLUSIVE_END | O.DISPATCH_BY_POINTS}
 
 

@@ -4,14 +4,19 @@ ships with the reference's vendored laszip (libs/laszip/example/5points_14.las,
 header fields decoded here with `struct` at the offsets the reference reads
 (LasLoaderSparse.cpp:493-526), independently of the library's parser.
 
-    python tests/golden/make_las_fixture.py [path to the reference checkout]
+    python tests/golden/make_las_fixture.py <path to the reference checkout>
+    (or CR_REFERENCE=<path> python tests/golden/make_las_fixture.py)
 """
 import json
+import os
 import struct
 import sys
 from pathlib import Path
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CR_REFERENCE")
+if not arg:
+    sys.exit("usage: make_las_fixture.py <path to the reference checkout> (or set CR_REFERENCE)")
+ref = Path(arg)
 data = (ref / "libs" / "laszip" / "example" / "5points_14.las").read_bytes()
 u = lambda fmt, off: struct.unpack_from("<" + fmt, data, off)[0]
 fields = {

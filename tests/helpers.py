@@ -8,7 +8,7 @@ from compute_rasterizer_gb300 import default_params, make_view, synth
 from oracle import oracle as O
 
 QUIRKS = {L.METHOD_LOOP_LAS: O.L0_X12,
-          L.METHOD_LOOP_LAS_PREFETCH: O.INCLUSIVE_END | O.DISPATCH_BY_POINTS,
+          L.METHOD_LOOP_LAS_PREFETCH: O.INCLUSIVE_END | O.DISPATCH_BY_POINTS | O.UVEC4_BASE,
           L.METHOD_LOOP_LAS_HQS: O.L0_X12 | O.INCLUSIVE_END | O.DISPATCH_BY_POINTS}
 
 
@@ -117,3 +117,96 @@ def build_method_demo(out_dir):
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
     return exe
+
+
+def many_file_cloud(nfiles=300, seed=11, extent=3000.0, base=10241, spread=2999):
+    """A terrain cut into `nfiles` LAS files the way the reference's loader
+    sees a tiled dataset: consecutive runs of the Morton-ordered records, each
+    file its own boxMin (the min of its points) and file_index, encoded by the
+    host layout builder at its sparse offset.  Every file holds more than
+    10,240 points (two batch records), and the file sizes vary, so the files'
+    first points fall on every value of firstPoint % 4."""
+    sizes = [base + (i * 7919) % spread for i in range(nfiles)]
+    n = int(sum(sizes))
+    p, rec, hdr = terrain_las(n, extent, seed)
+    scale = np.array(hdr.scale[:], np.float64)
+    offset = np.array(hdr.offset[:], np.float64)
+    rec2 = rec.reshape(n, L.LAS_FORMAT2_BYTES)
+    xyz = rec2[:, :12].copy().view("<i4").reshape(n, 3).astype(np.float64) * scale + offset
+    parts = [[], [], [], [], []]
+    box_mins = np.zeros((nfiles, 3), np.float64)
+    off = 0
+    for i, sz in enumerate(sizes):
+        bmin = xyz[off:off + sz].min(axis=0)
+        box_mins[i] = bmin
+        out = synth.encode_las(np.ascontiguousarray(rec2[off:off + sz]).reshape(-1), sz, hdr,
+                               sparse_offset=off, file_index=i, box_min=bmin)
+        for k in range(5):
+            parts[k].append(out[k])
+        off += sz
+    batches, lo, md, hi, rgba = (np.concatenate(x) for x in parts)
+    return dict(n=n, hdr=hdr, batches=batches, lo=lo, md=md, hi=hi, rgba=rgba,
+                box_min=box_mins, box_max=synth.header_max(hdr), world_min=synth.header_min(hdr),
+                sizes=sizes)
+
+
+def many_file_cameras(cl, width=480, height=270):
+    """far: the whole tiled cloud (10-bit); mid and near: 120 m and 5 m from
+    a batch centre of a file in the middle (levels 1-4, and 0-4: 20/30-bit
+    batches of several files next to 10-bit ones, the rest culled)."""
+    bmin, bmax = cl["world_min"], cl["box_max"]
+    yaw, pitch, radius, target = synth.zoom_to_cloud(bmin, bmax)
+    b = cl["batches"][len(cl["batches"]) // 2]
+    fmin = cl["box_min"][b["file_index"]]
+    centre = fmin + 0.5 * np.array([b["min_x"] + b["max_x"], b["min_y"] + b["max_y"],
+                                    b["min_z"] + b["max_z"]], np.float64)
+    proj = synth.perspective(60.0, width / height, 0.1, 200000.0)
+    views = {"far": synth.orbit_view(yaw, pitch, radius, target),
+             "mid": synth.orbit_view(1.1, -0.6, 120.0, centre),
+             "near": synth.orbit_view(0.3, -0.35, 5.0, centre)}
+    return {k: (v, proj, width, height) for k, v in views.items()}
+
+
+def pixel_grid_cloud(firsts, counts, total, width=1024, height=32):
+    """Batches over one stream whose point g (global index) decodes, under the
+    identity camera of a width x height view, to its own pixel
+    (g % width, g // width): X = g % 1024 (width 1024), Y = (g // 1024) * 32.
+    Every batch has the AABB (-1, -1, 0) - (1, 1, 1); `firsts` / `counts` are
+    the batches' first_point / num_points (any alignment).  A rendered index
+    payload therefore shows exactly which points a method visited."""
+    assert width == 1024 and height == 32 and total + 64 <= width * height
+    g = np.arange(total + 64, dtype=np.uint32)
+    lo = (g % 1024) | (((g // 1024) * 32) << 10)
+    lo[total:] = 0
+    b = np.zeros(len(firsts), L.BATCH_DTYPE)
+    b["min_x"], b["min_y"], b["min_z"] = -1.0, -1.0, 0.0
+    b["max_x"], b["max_y"], b["max_z"] = 1.0, 1.0, 1.0
+    b["first_point"] = firsts
+    b["num_points"] = counts
+    zeros = np.zeros(total + 64, np.uint32)
+    rgba = (g * 2654435761).astype(np.uint32) & np.uint32(0xFFFFFF)
+    return dict(n=total, batches=b, lo=lo.astype(np.uint32), md=zeros.copy(), hi=zeros.copy(),
+                rgba=rgba, box_min=np.zeros((1, 3)))
+
+
+def las2_visits(first, num_points, inclusive=True, threads=128, per_thread=80):
+    """The batch-local indices compute_loop_las2/render.cs:319-341 visits: per
+    thread base = firstPoint / 4 + tid, index = 4 * (base + i * 128) + j, uint
+    localIndex = index - firstPoint, `localIndex > numPoints` returns (`>=` when
+    not inclusive).  A literal restatement of the shader's loop, in Python."""
+    out = []
+    m = 0xFFFFFFFF
+    for t in range(threads):
+        base = first // 4 + t
+        done = False
+        for i in range(per_thread // 4):
+            for j in range(4):
+                index = (4 * (base + i * threads) + j) & m
+                local = (index - first) & m
+                if local > num_points or (not inclusive and local == num_points):
+                    done = True
+                    break
+                out.append(local)
+            if done:
+                break
+    return sorted(out)

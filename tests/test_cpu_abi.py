@@ -56,7 +56,7 @@ def test_method_registry_and_defaults():
     assert p.clear_value == L.DEFAULT_CLEAR
     lib.cr_render_params_default(L.METHOD_EARLYZ, C.byref(p))
     assert p.clear_value == L.PLAIN_RECLEAR
-    assert lib.cr_abi_version() == 1
+    assert lib.cr_abi_version() == 2
     assert lib.cr_status_string(L.DEVICE_FLAG) == b"device error flag raised"
 
 

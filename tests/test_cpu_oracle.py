@@ -373,7 +373,60 @@ def test_plain_byte_round_trip():
     fb = (rng.integers(1, 2**31, w * h + w + 1, dtype=np.uint64) << np.uint64(32)) | \
         rng.integers(0, 2**32, w * h + w + 1, dtype=np.uint64)
     fb[::5] &= np.uint64(0xFFFFFFFFFF000000)  # ucol == 0 -> (0, 0, 0, 255)
-    img = np.empty(w * h, dtype=np.uint32)
     ucol = (fb[: w * h] & np.uint64(0xFFFFFF)).astype(np.uint32)
-    O.lib().or_resolve_plain(w, h, fb.ctypes.data, img.ctypes.data, 0xFFFFFFFFFF3C321E)
-    assert np.array_equal(img, np.where(ucol == 0, np.uint32(0xFF000000), ucol))
+    for zero_rule in (1, 0):
+        img = np.empty(w * h, dtype=np.uint32)
+        f = fb.copy()
+        O.lib().or_resolve_plain(w, h, f.ctypes.data, img.ctypes.data, 0xFFFFFFFFFF3C321E, 0,
+                                 zero_rule)
+        # early-z: ucol == 0 -> (0,0,0,255); dedup (compute_2021_dedup/resolve.cs:15-21)
+        # has no such rule and writes the zero bytes
+        want = np.where(ucol == 0, np.uint32(0xFF000000), ucol) if zero_rule else ucol
+        assert np.array_equal(img, want)
+        assert (f == np.uint64(0xFFFFFFFFFF3C321E)).all()  # pixels and guard tail re-cleared
+
+
+def test_plain_resolve_tiles():
+    """compute_2021_earlyz.h:161-163 dispatches floor(W/16) x floor(H/16)
+    groups of 16x16: with the tile quirk, pixels past the last full tile keep
+    their image and framebuffer words (and the guard tail is untouched)."""
+    rng = np.random.default_rng(5)
+    w, h = 40, 35  # 2 x 2 full tiles: x < 32, y < 32 resolved
+    fb = (rng.integers(1, 2**31, w * h + w + 1, dtype=np.uint64) << np.uint64(32)) | \
+        rng.integers(1, 2**24, w * h + w + 1, dtype=np.uint64)
+    img0 = rng.integers(0, 2**32, w * h, dtype=np.uint64).astype(np.uint32)
+    img, f = img0.copy(), fb.copy()
+    O.lib().or_resolve_plain(w, h, f.ctypes.data, img.ctypes.data, 7, O.PLAIN_TILES, 1)
+    x, y = np.meshgrid(np.arange(w), np.arange(h))
+    inside = ((x < 32) & (y < 32)).reshape(-1)
+    ucol = (fb[: w * h] & np.uint64(0xFFFFFF)).astype(np.uint32)
+    assert np.array_equal(img[inside], ucol[inside])
+    assert np.array_equal(img[~inside], img0[~inside])
+    assert (f[: w * h][inside] == 7).all()
+    assert np.array_equal(f[: w * h][~inside], fb[: w * h][~inside])
+    assert np.array_equal(f[w * h:], fb[w * h:])
+
+
+def test_uvec4_base_matches_las2_thread_loop():
+    """H6 (compute_loop_las2/render.cs:319-341): the oracle's CR_QUIRK_UVEC4_BASE
+    rule renders exactly the points the shader's 128 threads visit, for
+    firstPoint % 4 = 0..3, full and partial batches, with and without the
+    inclusive end (H2)."""
+    from helpers import las2_visits, pixel_grid_cloud
+    firsts = [1, 10242, 20483, 26484]  # firstPoint % 4 = 1, 2, 3, 0
+    counts = [10240, 10240, 6000, 1000]
+    total = 27490
+    cl = pixel_grid_cloud(firsts, counts, total)
+    ident = np.eye(4).reshape(16)
+    for inclusive in (False, True):
+        q = O.UVEC4_BASE | (O.INCLUSIVE_END if inclusive else 0)
+        fr = O.make_frame(ident, ident, 1024, 32, cl["box_min"], culling=0, quirks=q)
+        fb = O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+        got = set(int(x) for x in (fb[:1024 * 32] & np.uint64(0xFFFFFFFF))) - {0xFF800000}
+        want = {f + l for f, c in zip(firsts, counts) for l in las2_visits(f, c, inclusive)}
+        assert got == want, (inclusive, sorted(want - got)[:8], sorted(got - want)[:8])
+        # without the quirk every point of [first, first + count) is rendered
+        fr0 = O.make_frame(ident, ident, 1024, 32, cl["box_min"], culling=0,
+                           quirks=O.INCLUSIVE_END if inclusive else 0)
+        fb0 = O.raster_batched(fr0, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+        assert (fb0 != fb).any()

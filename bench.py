@@ -326,7 +326,7 @@ def main():
     n = args.points
     W, H = WORKLOAD["width"], WORKLOAD["height"]
     sp = synth.synth_params(L.SYNTH_TERRAIN, WORKLOAD["extent"], WORKLOAD["seed"] + rank)
-    cloud, hdr = synth.build_cloud_device(ctx, sp, n, sh)
+    cloud, hdr, build_ms = synth.build_cloud_device_timed(ctx, sp, n, sh)
     bmin, bmax = np.array(hdr.min[:]), np.array(hdr.max[:])
     view, proj = camera(bmin, bmax, W, H)
     cv = cr.make_view(view, proj, W, H)
@@ -398,7 +398,10 @@ def main():
            "clocks": clk}
 
     if not args.no_extras:
-        out["extras"] = {}
+        out["extras"] = {"cloud_build": {
+            "points": n, "ms": build_ms,
+            "what": "GPU generator (LAS records) -> Morton sort (radix sort + gather) -> "
+                    "LAS-derived layout encoder, CUDA events per stage; outside the timed frames"}}
         want = set(args.extras.split(","))
         runs = [("payloads", lambda: extras(ctx, cloud, cv, fb, sh, n, args)),
                 ("multiview", lambda: {"multiview_64": multiview_64(ctx, sh, args.steps, payload)}),

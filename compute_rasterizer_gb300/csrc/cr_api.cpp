@@ -906,7 +906,8 @@ cr_status cr_encode_las(const uint8_t* rec, int64_t n, int32_t bpp, int32_t fmt,
                         int32_t file_index, cr_batch* batches, uint32_t* lo, uint32_t* md,
                         uint32_t* hi, uint32_t* rgba) {
     if ((n > 0 && !rec) || n < 0 || bpp < 12 || !scale || !offset || !box_min || !batches || !lo ||
-        !md || !hi || !rgba || sparse_offset < 0 || sparse_offset + n >= ((int64_t)1 << 31))
+        !md || !hi || !rgba || sparse_offset < 0 || sparse_offset + n >= ((int64_t)1 << 31) ||
+        !finite_all(scale, 3) || !finite_all(offset, 3) || !finite_all(box_min, 3))
         return CR_ERR_INVALID_ARG;
     // LasLoaderSparse.cpp:123-132
     const int rgb = fmt == 2 ? 20 : (fmt == 3 ? 28 : ((fmt == 7 || fmt == 8) ? 30 : 0));

@@ -155,15 +155,31 @@ __host__ __device__ inline int32_t get_i32(const uint8_t* d) {
 }
 __host__ __device__ inline uint32_t get_u16(const uint8_t* d) { return (uint32_t)d[0] | ((uint32_t)d[1] << 8); }
 
+// floor(x / s + 0.5) (the LAS integer of a coordinate), bit for bit, with the
+// division replaced by a multiplication with inv = RN(1/s) where that cannot
+// change the result: x * inv lies within 3 ulps of RN(x / s) and
+// r -> floor(RN(r + 0.5)) is monotone, so when both ends of a margin of 8
+// ulps around the product give the same integer, so does RN(x / s).  Near a
+// half-integer the division is done.  (Double division runs at a small
+// fraction of the FP64 rate on this part.)
+__host__ __device__ inline int32_t las_int(double x, double s, double inv) {
+    const double r1 = x * inv;
+    const double e = fabs(r1) * 0x1p-49;
+    const double lo = floor((r1 - e) + 0.5), hi = floor((r1 + e) + 0.5);
+    return (int32_t)(lo == hi ? lo : floor(x / s + 0.5));
+}
+
 // One LAS point-format-2 record (26 B).  Colors are stored as 16-bit values
 // (c * 256) for 7 of 8 points and as plain 8-bit values for the rest, so both
 // branches of the loader's `v < 256 ? v : v / 256` are exercised.
-__host__ __device__ inline void write_record(const cr_synth_params& p, int64_t n, uint64_t i, uint8_t* d) {
+// inv_scale = 1 / p.las_scale.
+__host__ __device__ inline void write_record(const cr_synth_params& p, double inv_scale, int64_t n,
+                                             uint64_t i, uint8_t* d) {
     GenPoint g;
     gen_point(p, n, i, g);
-    const int32_t X = (int32_t)floor(g.x / p.las_scale + 0.5);
-    const int32_t Y = (int32_t)floor(g.y / p.las_scale + 0.5);
-    const int32_t Z = (int32_t)floor(g.z / p.las_scale + 0.5);
+    const int32_t X = las_int(g.x, p.las_scale, inv_scale);
+    const int32_t Y = las_int(g.y, p.las_scale, inv_scale);
+    const int32_t Z = las_int(g.z, p.las_scale, inv_scale);
     put_i32(d + 0, X);
     put_i32(d + 4, Y);
     put_i32(d + 8, Z);
@@ -243,10 +259,10 @@ bool valid_params(const cr_synth_params* p) {
 
 // ---- device kernels ------------------------------------------------------------
 
-__global__ void k_gen(cr_synth_params p, int64_t n, uint8_t* rec) {
+__global__ void k_gen(cr_synth_params p, double inv_scale, int64_t n, uint8_t* rec) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
-        write_record(p, n, (uint64_t)i, rec + i * kRecBytes);
+        write_record(p, inv_scale, n, (uint64_t)i, rec + i * kRecBytes);
 }
 
 __global__ void k_bounds(const uint8_t* rec, int64_t n, int32_t bpp, int32_t* mnmx) {
@@ -281,12 +297,41 @@ __global__ void k_morton_keys(MortonFrame f, const uint8_t* rec, int64_t n, int3
     }
 }
 
-__global__ void k_gather(const uint8_t* src, uint8_t* dst, const uint32_t* perm, int64_t n, int32_t bpp) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t* s = src + (int64_t)perm[i] * bpp;
-        uint8_t* d = dst + i * bpp;
-        for (int k = 0; k < bpp; k++) d[k] = s[k];
+// dst[i] = src[perm[i]] for records of `bpp` bytes (even, <= kGatherMaxBpp).
+// A warp gathers 32 records: each lane reads its source record as 16-bit
+// words (records start on 2-byte boundaries), writes them into the warp's
+// slice of shared memory at their destination offsets, and the warp stores the
+// 32 * bpp contiguous destination bytes as 16-byte vectors (bpp is even, so
+// 32 * bpp is a multiple of 16 and the warp's first byte is 16-byte aligned
+// when dst is).  The tail warp (fewer than 32 records) stores 16-bit words.
+constexpr int kGatherMaxBpp = 64;
+constexpr int kGatherWarps = 8;
+__global__ void __launch_bounds__(32 * kGatherWarps) k_gather(const uint8_t* __restrict__ src,
+                                                              uint8_t* __restrict__ dst,
+                                                              const uint32_t* __restrict__ perm,
+                                                              int64_t n, int32_t bpp) {
+    __shared__ __align__(16) uint16_t s_buf[kGatherWarps][32 * kGatherMaxBpp / 2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint16_t* buf = s_buf[warp];
+    const int words = bpp >> 1;
+    const int64_t nwarps = (int64_t)gridDim.x * kGatherWarps;
+    for (int64_t w0 = ((int64_t)blockIdx.x * kGatherWarps + warp) * 32; w0 < n; w0 += nwarps * 32) {
+        const int64_t i = w0 + lane;
+        const int cnt = (int)min((int64_t)32, n - w0);
+        if (lane < cnt) {
+            const uint16_t* s = reinterpret_cast<const uint16_t*>(src + (int64_t)perm[i] * bpp);
+            for (int k = 0; k < words; k++) buf[lane * words + k] = __ldg(s + k);
+        }
+        __syncwarp();
+        uint8_t* d = dst + w0 * bpp;
+        if (cnt == 32) {
+            const int vecs = (32 * bpp) >> 4;
+            for (int k = lane; k < vecs; k += 32)
+                reinterpret_cast<uint4*>(d)[k] = reinterpret_cast<const uint4*>(buf)[k];
+        } else {
+            for (int k = lane; k < cnt * words; k += 32) reinterpret_cast<uint16_t*>(d)[k] = buf[k];
+        }
+        __syncwarp();
     }
 }
 
@@ -296,30 +341,47 @@ struct EncodeArgs {
     int32_t bpp, rgb, file_index;
 };
 
+// LasLoaderSparse.cpp:146-148: min(uint32(((v - min) / size) * 2^30), 2^30 - 1)
+// (NaN -> 0), bit for bit, with one multiplication by inv = RN(1/size) in
+// place of the division where that cannot change the result: d * inv lies
+// within 3 ulps of RN(d / size), so when no integer lies within 8 ulps of
+// t1 = d * inv * 2^30 both truncate to the same integer.  Otherwise (a point
+// on the box's far face, about one in 2^20 others, a zero or subnormal size)
+// the division is done.
+__device__ __forceinline__ uint32_t quantize30(double d, double size, double inv) {
+    const double t1 = (d * inv) * 1073741824.0;
+    const double e = t1 * 0x1p-49;
+    double t = t1;
+    if (!(floor(t1 - e) == floor(t1 + e))) t = (d / size) * 1073741824.0;
+    const uint32_t u = (t != t) ? 0u : (uint32_t)t;
+    return u < 1073741823u ? u : 1073741823u;
+}
+
 // LasLoaderSparse.cpp:84-199, one CTA per batch.
 __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __restrict__ rec,
                                                 cr_batch* batches, uint32_t* lo, uint32_t* md,
                                                 uint32_t* hi, uint32_t* rgba) {
-    __shared__ double s_red[6][8];
-    __shared__ double s_box[6];
+    __shared__ int32_t s_red[6][8];
+    __shared__ double s_box[9];
     const int64_t first = (int64_t)blockIdx.x * cr::kPointsPerBatch;
     const int64_t left = a.n - first;
     const int cnt = (int)(left < cr::kPointsPerBatch ? left : cr::kPointsPerBatch);
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    // The batch AABB of v = double(X) * scale + offset - boxMin
+    // (LasLoaderSparse.cpp:93-105): every step rounds monotonically, so v is
+    // monotone in the integer X and the box is v at the integer extremes.
+    int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
         const uint8_t* r = rec + (first + i) * a.bpp;
         for (int k = 0; k < 3; k++) {
-            const double v = (double)get_i32(r + 4 * k) * a.scale[k] + a.offset[k] - a.box_min[k];
-            mn[k] = v < mn[k] ? v : mn[k];
-            mx[k] = mx[k] < v ? v : mx[k];
+            const int32_t X = get_i32(r + 4 * k);
+            mn[k] = min(mn[k], X);
+            mx[k] = max(mx[k], X);
         }
     }
     for (int o = 16; o > 0; o >>= 1)
         for (int k = 0; k < 3; k++) {
-            const double m0 = __shfl_xor_sync(0xFFFFFFFFu, mn[k], o);
-            const double m1 = __shfl_xor_sync(0xFFFFFFFFu, mx[k], o);
-            mn[k] = m0 < mn[k] ? m0 : mn[k];
-            mx[k] = mx[k] < m1 ? m1 : mx[k];
+            mn[k] = min(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
         }
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     if ((threadIdx.x & 31) == 0)
@@ -328,18 +390,24 @@ __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __r
             s_red[3 + k][warp] = mx[k];
         }
     __syncthreads();
-    if (threadIdx.x < 6) {
+    if (threadIdx.x < 3) {
         const int k = threadIdx.x;
-        double v = s_red[k][0];
+        int32_t lo = s_red[k][0], hi = s_red[3 + k][0];
         for (int w = 1; w < nwarps; w++) {
-            const double u = s_red[k][w];
-            v = k < 3 ? (u < v ? u : v) : (v < u ? u : v);
+            lo = min(lo, s_red[k][w]);
+            hi = max(hi, s_red[3 + k][w]);
         }
-        s_box[k] = v;
+        const double vlo = (double)lo * a.scale[k] + a.offset[k] - a.box_min[k];
+        const double vhi = (double)hi * a.scale[k] + a.offset[k] - a.box_min[k];
+        const double b0 = a.scale[k] < 0.0 ? vhi : vlo, b1 = a.scale[k] < 0.0 ? vlo : vhi;
+        s_box[k] = b0;
+        s_box[3 + k] = b1;
+        s_box[6 + k] = 1.0 / (b1 - b0);
     }
     __syncthreads();
     const double bmin[3] = {s_box[0], s_box[1], s_box[2]};
     const double size[3] = {s_box[3] - s_box[0], s_box[4] - s_box[1], s_box[5] - s_box[2]};
+    const double inv[3] = {s_box[6], s_box[7], s_box[8]};
     if (threadIdx.x == 0) {
         cr_batch b;
         memset(&b, 0, sizeof(b));
@@ -356,9 +424,7 @@ __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __r
         uint32_t q[3];
         for (int k = 0; k < 3; k++) {
             const double v = (double)get_i32(r + 4 * k) * a.scale[k] + a.offset[k] - a.box_min[k];
-            const double t = ((v - bmin[k]) / size[k]) * 1073741824.0;
-            const uint32_t u = (t != t) ? 0u : (uint32_t)t;
-            q[k] = u < 1073741823u ? u : 1073741823u;
+            q[k] = quantize30(v - bmin[k], size[k], inv[k]);
         }
         lo[pi] = ((q[0] >> 20) & 1023u) | (((q[1] >> 20) & 1023u) << 10) | (((q[2] >> 20) & 1023u) << 20);
         md[pi] = ((q[0] >> 10) & 1023u) | (((q[1] >> 10) & 1023u) << 10) | (((q[2] >> 10) & 1023u) << 20);
@@ -431,8 +497,9 @@ void cr_synth_params_default(int32_t kind, double extent, uint64_t seed, cr_synt
 cr_status cr_synth_points_host(const cr_synth_params* p, int64_t n, uint8_t* rec, cr_las_header* hdr) {
     if (!valid_params(p) || n < 0 || (n > 0 && !rec) || !hdr) return CR_ERR_INVALID_ARG;
     const cr_synth_params pp = *p;
+    const double inv = 1.0 / pp.las_scale;
     parallel_for(n, [&](int64_t a, int64_t b) {
-        for (int64_t i = a; i < b; i++) write_record(pp, n, (uint64_t)i, rec + i * kRecBytes);
+        for (int64_t i = a; i < b; i++) write_record(pp, inv, n, (uint64_t)i, rec + i * kRecBytes);
     });
     int32_t mn[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, mx[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
     for (int64_t i = 0; i < n; i++)
@@ -473,7 +540,8 @@ cr_status cr_synth_points_device(cr_ctx* ctx, const cr_synth_params* p, int64_t 
     cudaError_t e = cudaMalloc(&d_mm, sizeof(init));
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_mm, init, sizeof(init), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && n > 0) {
-        k_gen<<<grid_for(n) * 4 > 65535 ? 65535 : grid_for(n) * 4, 256, 0, s>>>(*p, n, d_rec);
+        k_gen<<<grid_for(n) * 4 > 65535 ? 65535 : grid_for(n) * 4, 256, 0, s>>>(*p, 1.0 / p->las_scale,
+                                                                                 n, d_rec);
         k_bounds<<<grid_for(n) > 2048 ? 2048 : grid_for(n), 256, 0, s>>>(d_rec, n, kRecBytes, d_mm);
         e = cudaGetLastError();
     }
@@ -490,7 +558,8 @@ cr_status cr_synth_points_device(cr_ctx* ctx, const cr_synth_params* p, int64_t 
 
 cr_status cr_morton_sort_device(cr_ctx* ctx, uint8_t* d_rec, int64_t n, int32_t bpp,
                                 const cr_las_header* hdr, void* stream) {
-    if (!ctx || n < 0 || (n > 0 && !d_rec) || bpp < 12 || !hdr || n >= ((int64_t)1 << 31))
+    if (!ctx || n < 0 || (n > 0 && !d_rec) || bpp < 12 || (bpp & 1) || bpp > kGatherMaxBpp || !hdr ||
+        n >= ((int64_t)1 << 31))
         return CR_ERR_INVALID_ARG;
     if (n <= 1) return CR_OK;
     cudaStream_t s = (cudaStream_t)stream;
@@ -517,7 +586,9 @@ cr_status cr_morton_sort_device(cr_ctx* ctx, uint8_t* d_rec, int64_t n, int32_t 
         e = cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, keys, vals, (int)n, 0, 63, s);
     if (e == cudaSuccess) e = cudaMalloc(&tmp, (size_t)n * bpp);
     if (e == cudaSuccess) {
-        k_gather<<<grid_for(n), 256, 0, s>>>(d_rec, tmp, vals.Current(), n, bpp);
+        const int64_t warps = (n + 31) / 32;
+        const int grid = (int)std::min<int64_t>((warps + kGatherWarps - 1) / kGatherWarps, 65535);
+        k_gather<<<grid, 32 * kGatherWarps, 0, s>>>(d_rec, tmp, vals.Current(), n, bpp);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_rec, tmp, (size_t)n * bpp, cudaMemcpyDeviceToDevice, s);
@@ -537,6 +608,9 @@ cr_status cr_encode_las_device(cr_ctx* ctx, const uint8_t* d_rec, int64_t n, int
         !d_batches || !d_lo || !d_md || !d_hi || !d_rgba || sparse_offset < 0 ||
         sparse_offset + n >= ((int64_t)1 << 31))
         return CR_ERR_INVALID_ARG;
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(scale[k]) || !std::isfinite(offset[k]) || !std::isfinite(box_min[k]))
+            return CR_ERR_INVALID_ARG;
     const int rgb = fmt == 2 ? 20 : (fmt == 3 ? 28 : ((fmt == 7 || fmt == 8) ? 30 : 0));
     if (rgb != 0 && rgb + 6 > bpp) return CR_ERR_INVALID_ARG;
     const int64_t nb = cr_num_batches(n);

@@ -121,6 +121,40 @@ def build_cloud_device(ctx, params: L.SynthParams, n: int, stream=None):
     return cloud, hdr
 
 
+def build_cloud_device_timed(ctx, params: L.SynthParams, n: int, stream=None):
+    """build_cloud_device stage by stage (generate, Morton sort, encode), each
+    timed with CUDA events on `stream` -> (Cloud, header, {stage: ms})."""
+    import torch
+    lib = L.load()
+    cloud = ctx.cloud(n, int(lib.cr_num_batches(n)), 1)
+    hdr = L.LasHeader()
+    rec = torch.empty(n * L.LAS_FORMAT2_BYTES, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    torch.cuda.synchronize()
+    ev[0].record(st)
+    ctx.check(lib.cr_synth_points_device(ctx.handle, C.byref(params), n, rec.data_ptr(),
+                                         C.byref(hdr), stream), "generate")
+    ev[1].record(st)
+    ctx.check(lib.cr_morton_sort_device(ctx.handle, rec.data_ptr(), n, L.LAS_FORMAT2_BYTES,
+                                        C.byref(hdr), stream), "Morton sort")
+    ev[2].record(st)
+    d = cloud.device_pointers()
+    sc, of, mn = (np.ascontiguousarray(x[:], np.float64) for x in (hdr.scale, hdr.offset, hdr.min))
+    ctx.check(lib.cr_encode_las_device(ctx.handle, rec.data_ptr(), n, L.LAS_FORMAT2_BYTES, 2,
+                                       ptr(sc), ptr(of), ptr(mn), 0, 0, d["batches"], d["low"],
+                                       d["med"], d["hig"], d["rgba"], stream), "encode")
+    ev[3].record(st)
+    ctx.sync(stream)
+    cloud.set_files(mn)
+    del rec
+    torch.cuda.empty_cache()
+    ms = {k: round(ev[i].elapsed_time(ev[i + 1]), 2)
+          for i, k in enumerate(("generate", "morton_sort", "encode"))}
+    ms["total"] = round(sum(ms.values()), 2)
+    return cloud, hdr, ms
+
+
 def uniform_cloud_device(ctx, seed: int, n: int, size: float = 100.0, stream=None):
     cloud = ctx.plain_cloud_empty(n)
     ctx.check(L.load().cr_synth_uniform_device(ctx.handle, seed, n, size, cloud.vertices_pointer(),

@@ -66,7 +66,8 @@ cr_status cr_morton_sort_host(uint8_t* records, int64_t n, int32_t bytes_per_poi
  * bounds on the device and synchronizes `stream` to return them. */
 cr_status cr_synth_points_device(cr_ctx* ctx, const cr_synth_params* p, int64_t n,
                                  uint8_t* d_records, cr_las_header* hdr, void* stream);
-/* Device Morton sort (stable radix sort of (code, index), then a gather). */
+/* Device Morton sort (stable radix sort of (code, index), then a gather);
+ * records of an even bytes_per_point in [12, 64], as LAS point formats are. */
 cr_status cr_morton_sort_device(cr_ctx* ctx, uint8_t* d_records, int64_t n,
                                 int32_t bytes_per_point, const cr_las_header* hdr, void* stream);
 /* GPU encoder: loadLas (LasLoaderSparse.cpp:37-212) over device records, one

@@ -21,10 +21,12 @@ OK, INVALID_ARG, OUT_OF_MEMORY, ADMISSION_REJECTED, TIMEOUT, CUDA_ERROR, DEVICE_
 
 # methods / payloads / quirks / streams / fb kinds
 METHOD_LOOP_LAS, METHOD_LOOP_LAS_PREFETCH, METHOD_LOOP_LAS_HQS, METHOD_EARLYZ, METHOD_DEDUP, \
-    METHOD_EARLYZ_REDUCE = range(6)
+    METHOD_EARLYZ_REDUCE, METHOD_LOOP_NODES = range(7)
 PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
-QUIRK_L0_X12, QUIRK_INCLUSIVE_END, QUIRK_DISPATCH_BY_POINTS, QUIRK_UVEC4_BASE, QUIRK_PLAIN_TILES = \
+QUIRK_L0_X12, QUIRK_INCLUSIVE_END, QUIRK_DISPATCH_BY_POINTS, QUIRK_UVEC4_BASE, QUIRK_RESOLVE_TILES = \
     1, 2, 4, 8, 16
+QUIRK_NODE_LOOP, QUIRK_LEVEL4_80PX, QUIRK_ONE_WORLD, QUIRK_FLOAT_UNIFORMS = 32, 64, 128, 256
+POTREE_QUIRK_12B_FROM_8B, POTREE_QUIRK_WRAP30, POTREE_QUIRKS_DEFAULT = 1, 2, -1
 MAX_FILES = 65536
 NOALLOC_MAX_BATCHES, NOALLOC_MAX_FILES, NOALLOC_SCRATCH_BYTES = 131064, 1024, 753664
 QUIRKS_METHOD_DEFAULT = -1
@@ -111,6 +113,20 @@ class ServerStats(C.Structure):
                 ("pool_bytes", C.c_int64), ("pool_used_bytes", C.c_int64),
                 ("pool_peak_bytes", C.c_int64), ("max_views_in_launch", C.c_int32),
                 ("queued", C.c_int32), ("gpu_ms", C.c_double)]
+
+
+class PotreeInfo(C.Structure):
+    _fields_ = [("num_points", C.c_int64), ("num_nodes", C.c_int64), ("octree_bytes", C.c_int64),
+                ("bytes_per_point", C.c_int32), ("rgb_offset", C.c_int32), ("max_level", C.c_int32),
+                ("reserved", C.c_int32), ("max_node_points", C.c_int64),
+                ("scale", C.c_double * 3), ("offset", C.c_double * 3),
+                ("box_min", C.c_double * 3), ("box_max", C.c_double * 3), ("spacing", C.c_double)]
+
+
+class PotreeNode(C.Structure):
+    _fields_ = [("level", C.c_int32), ("type", C.c_int32), ("child_mask", C.c_int32),
+                ("reserved", C.c_int32), ("num_points", C.c_int64), ("byte_offset", C.c_int64),
+                ("byte_size", C.c_int64), ("min", C.c_double * 3), ("max", C.c_double * 3)]
 
 
 class LasInfo(C.Structure):
@@ -202,6 +218,11 @@ _SIGS = {
     "cr_synth_uniform_device": (I32, [P, U64, I64, FLT, P, P]),
     # cr_las.h
     "cr_las_parse_header": (I32, [P, I64, C.POINTER(LasInfo)]),
+    "cr_potree_open": (I32, [C.c_char_p, PP, C.POINTER(PotreeInfo)]),
+    "cr_potree_close": (I32, [P]),
+    "cr_potree_nodes": (I32, [P, P, I64]),
+    "cr_potree_encode": (I32, [P, P, I64, I32, P, P, P, P, P]),
+    "cr_potree_load": (I32, [P, P, I32, PP, P]),
     "cr_cloud_load_las": (I32, [P, P, P, I64, C.POINTER(LasInfo), I64, I64, I32, P]),
     "cr_las_num_batches": (I64, [I64]),
     # cr_serve.h

@@ -17,7 +17,8 @@ OUT = PKG / "_build"
 LIB = OUT / "libcr_raster.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-SOURCES = ["cr_api.cpp", "cr_kernels.cu", "cr_synth.cu", "cr_noalloc.cu", "cr_multiview.cu", "cr_serve.cpp", "cr_las.cpp"]
+SOURCES = ["cr_api.cpp", "cr_kernels.cu", "cr_synth.cu", "cr_noalloc.cu", "cr_multiview.cu", "cr_serve.cpp",
+           "cr_las.cpp", "cr_potree.cpp"]
 
 # -fmad=false: no implicit contraction; explicit __fmaf_rn only.
 NVCC_FLAGS = [

@@ -102,7 +102,7 @@ bool finite_all(const double* v, int n) {
 }
 
 cr_status build_view_params(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view, int culling,
-                            ViewParams* vp) {
+                            int quirks, ViewParams* vp) {
     if (!finite_all(view->view, 16) || !finite_all(view->proj, 16))
         return fail(ctx, CR_ERR_INVALID_ARG, "view matrices must be finite%s", "");
     std::memset(vp, 0, sizeof(*vp));
@@ -111,14 +111,20 @@ cr_status build_view_params(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* v
     vp->H = view->height;
     vp->nfiles = cloud->nfiles;
     vp->culling = culling ? 1 : 0;
-    for (int f = 0; f < std::min(cloud->nfiles, kInlineFiles); f++)
-        file_record(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f]);
+    vp->level4_px = (quirks & CR_QUIRK_LEVEL4_80PX) ? 80.0f : 100.0f;
+    vp->one_world = (quirks & CR_QUIRK_ONE_WORLD) ? 1 : 0;
+    for (int f = 0; f < std::min(cloud->nfiles, kInlineFiles); f++) {
+        if (quirks & CR_QUIRK_FLOAT_UNIFORMS)
+            file_record_float(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f]);
+        else
+            file_record(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f]);
+    }
     return CR_OK;
 }
 
 // Clouds with more than kInlineFiles files: every file's record of this view,
 // computed on the GPU on `stream` into the context's record array.
-cr_status enqueue_file_records(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
+cr_status enqueue_file_records(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view, int quirks,
                                ViewParams* vp, void* stream) {
     if (cloud->nfiles <= kInlineFiles) return CR_OK;
     if (ctx->files_cap < cloud->nfiles) {
@@ -133,7 +139,7 @@ cr_status enqueue_file_records(cr_ctx* ctx, const cr_cloud* cloud, const cr_view
         ctx->files_cap = cloud->nfiles;
     }
     if (launch_file_records(view->view, view->proj, cloud->box_min.data(), cloud->nfiles, ctx->files,
-                            stream) != 0)
+                            stream, (quirks & CR_QUIRK_FLOAT_UNIFORMS) ? 1 : 0) != 0)
         return fail(ctx, CR_ERR_CUDA, "file record launch failed%s", "");
     vp->dfiles = ctx->files;
     return CR_OK;
@@ -164,13 +170,15 @@ cr_status ensure_scratch(cr_ctx* ctx, int64_t items) {
     return CR_OK;
 }
 
-constexpr int kNumMethods = 6;
+constexpr int kNumMethods = 7;
 const char* kNames[kNumMethods] = {"loop_las",       "loop_las_prefetch", "loop_las_hqs",
-                                   "(2021) early-z", "(2021) dedup",      "(2021) early-z & reduce"};
+                                   "(2021) early-z", "(2021) dedup",      "(2021) early-z & reduce",
+                                   "loop_nodes"};
 const char* kGroups[kNumMethods] = {"10-10-10 bit encoded", "10-10-10 bit encoded", "10-10-10 bit encoded",
                                     "2021 method; standard 16 byte per point",
                                     "2021 method; standard 16 byte per point",
-                                    "2021 method; standard 16 byte per point"};
+                                    "2021 method; standard 16 byte per point",
+                                    "render Potree nodes"};
 const char* kDescriptions[kNumMethods] = {
     "Batched atomicMin rasterizer over the 10-10-10 bit encoded layout; each batch picks 10, 20 "
     "or 30 bit coordinates from its projected size; point-index payload.",
@@ -181,7 +189,9 @@ const char* kDescriptions[kNumMethods] = {
     "Plain 16 byte per point layout; the points of a warp are partitioned by pixel and only each "
     "partition's closest point is written (depth<<24|color).",
     "Plain 16 byte per point layout; a warp on one pixel writes only its closest point, otherwise "
-    "pairs of lanes drop the farther of two points on one pixel (depth<<24|color)."};
+    "pairs of lanes drop the farther of two points on one pixel (depth<<24|color).",
+    "Potree octree nodes as batches of up to 64,512 points, 10/20/30 bit coordinates per node; "
+    "nodes below 80 pixels (level 4) are skipped."};
 
 bool plain_method(int32_t m) {
     return m == CR_METHOD_EARLYZ || m == CR_METHOD_DEDUP || m == CR_METHOD_EARLYZ_REDUCE;
@@ -196,7 +206,10 @@ int default_quirks(int32_t method) {
             return CR_QUIRK_L0_X12 | CR_QUIRK_INCLUSIVE_END | CR_QUIRK_DISPATCH_BY_POINTS;
         case CR_METHOD_EARLYZ:
         case CR_METHOD_DEDUP:
-        case CR_METHOD_EARLYZ_REDUCE: return CR_QUIRK_PLAIN_TILES;
+        case CR_METHOD_EARLYZ_REDUCE: return CR_QUIRK_RESOLVE_TILES;
+        case CR_METHOD_LOOP_NODES:
+            return CR_QUIRK_NODE_LOOP | CR_QUIRK_LEVEL4_80PX | CR_QUIRK_ONE_WORLD |
+                   CR_QUIRK_FLOAT_UNIFORMS | CR_QUIRK_RESOLVE_TILES;
         default: return 0;
     }
 }
@@ -240,6 +253,7 @@ cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_
     vp->H = view->height;
     vp->nfiles = num_files;
     vp->culling = culling ? 1 : 0;
+    vp->level4_px = 100.0f;
     for (int f = 0; f < std::min(num_files, kInlineFiles); f++)
         file_record(view->view, view->proj, &box_min[3 * f], &vp->files[f]);
     return CR_OK;
@@ -291,6 +305,7 @@ void cr_render_params_default(int32_t method, cr_render_params* out) {
     out->resolve = 1;
     out->clear_after = 1;
     out->clear_value = plain_method(method) ? kPlainReclear : kDefaultClear;
+    if (method == CR_METHOD_LOOP_NODES) out->lod_skip_level = 4;  // compute_loop_nodes/render.cs:273
 }
 
 // ---- context ----------------------------------------------------------------
@@ -714,15 +729,22 @@ cr_status cr_resolve(cr_ctx* ctx, const cr_cloud* cloud, const cr_render_params*
         if (plain_method(p->method)) {
             const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? default_quirks(p->method) : p->quirks;
             rc = launch_resolve_plain(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value,
-                                      (quirks & CR_QUIRK_PLAIN_TILES) != 0,
+                                      (quirks & CR_QUIRK_RESOLVE_TILES) != 0,
                                       p->method != CR_METHOD_DEDUP, stream);
-        } else if (p->payload == CR_PAYLOAD_COLOR) {
-            rc = launch_resolve_color(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value, stream);
         } else {
-            if (!cloud || !cloud->rgba)
-                return fail(ctx, CR_ERR_INVALID_ARG, "index payload resolve needs the color stream%s", "");
-            rc = launch_resolve_index(fb->W, fb->H, fb->fb, cloud->rgba, cloud->capacity, fb->image,
-                                      p->clear_after, p->clear_value, stream);
+            const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? default_quirks(p->method) : p->quirks;
+            const int tiles = (quirks & CR_QUIRK_RESOLVE_TILES) ? 1 : 0;
+            if (p->payload == CR_PAYLOAD_COLOR && !tiles) {
+                rc = launch_resolve_color(fb->W, fb->H, fb->fb, fb->image, p->clear_after, p->clear_value,
+                                          stream);
+            } else if (p->payload == CR_PAYLOAD_COLOR) {
+                return fail(ctx, CR_ERR_UNSUPPORTED, "the tiled resolve reads the index payload%s", "");
+            } else {
+                if (!cloud || !cloud->rgba)
+                    return fail(ctx, CR_ERR_INVALID_ARG, "index payload resolve needs the color stream%s", "");
+                rc = launch_resolve_index(fb->W, fb->H, fb->fb, cloud->rgba, cloud->capacity, fb->image,
+                                          p->clear_after, p->clear_value, stream, tiles);
+            }
         }
     }
     if (rc != 0) return fail(ctx, CR_ERR_CUDA, "resolve launch failed%s", "");
@@ -796,10 +818,10 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     }
 
     ViewParams vp;
-    s = build_view_params(ctx, cloud, view, p->frustum_culling, &vp);
+    s = build_view_params(ctx, cloud, view, p->frustum_culling, quirks, &vp);
     if (s != CR_OK) return s;
     vp.lod_skip_level = p->lod_skip_level;
-    s = enqueue_file_records(ctx, cloud, view, &vp, stream);
+    s = enqueue_file_records(ctx, cloud, view, quirks, &vp, stream);
     if (s != CR_OK) return s;
     // the loader's numBatchesLoaded / numPointsLoaded (compute_loop_las.h:233,
     // compute_loop_las2.h:234)
@@ -885,8 +907,13 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
         const uint32_t b = it & kItemBatchMask;
         const int level = (int)(it >> 29);
         if (b >= recs.size() || level > 4) continue;
-        int64_t n = recs[b].num_points + ((quirks & CR_QUIRK_INCLUSIVE_END) ? 1 : 0);
-        n = std::min<int64_t>(n, kPointsPerBatch);
+        int64_t n = recs[b].num_points;
+        if (quirks & CR_QUIRK_NODE_LOOP) {  // compute_loop_nodes/render.cs:296-300
+            const int64_t loop = std::min<int64_t>((n + 127) / 128, 500);
+            n = std::min<int64_t>(n, 512 * ((loop + 4) / 4) - (recs[b].first_point & 3));
+        } else {
+            n = std::min<int64_t>(n + ((quirks & CR_QUIRK_INCLUSIVE_END) ? 1 : 0), kPointsPerBatch);
+        }
         const int words = level >= 2 ? 1 : (level == 1 ? 2 : 3);
         out->batches_per_level[level] += 1;
         out->points_per_level[level] += n;

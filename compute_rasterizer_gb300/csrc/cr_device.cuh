@@ -137,8 +137,11 @@ __device__ void mat4_vec4(const float* m, const float v[4], float o[4]) {
     }
 }
 
+// lvl4_px: the pixel size below which a batch is level 4 (render.cs:217 100,
+// compute_loop_nodes/render.cs:199 80)
 __device__ int precision_level(const float* P, const float* VW, int32_t W, int32_t H, float mnx,
-                               float mny, float mnz, float mxx, float mxy, float mxz) {
+                               float mny, float mnz, float mxx, float mxy, float mxz,
+                               float lvl4_px = 100.0f) {
     float c[4] = {__fdiv_rn(fadd(mnx, mxx), 2.0f), __fdiv_rn(fadd(mny, mxy), 2.0f),
                   __fdiv_rn(fadd(mnz, mxz), 2.0f), 1.0f};
     float dx = fsub(mnx, mxx), dy = fsub(mny, mxy), dz = fsub(mnz, mxz);
@@ -162,15 +165,26 @@ __device__ int precision_level(const float* P, const float* VW, int32_t W, int32
     float sey = __fdiv_rn(fmul(Hf, fadd(pey, 1.0f)), 2.0f);
     float ex = fsub(sex, scx), ey = fsub(sey, scy);
     float px = __fsqrt_rn(fadd(fmul(ex, ex), fmul(ey, ey)));
-    if (px < 100.0f) return 4;
+    if (px < lvl4_px) return 4;
     if (px < 200.0f) return 3;
     if (px < 500.0f) return 2;
     if (px < 10000.0f) return 1;
     return 0;
 }
 
-__device__ __forceinline__ int64_t points_in_batch(int32_t num_points, int32_t quirks) {
+// Points a batch's loop visits, from its first point: num_points (+1 with the
+// inclusive end), at most 10,240; with CR_QUIRK_NODE_LOOP the loop of
+// compute_loop_nodes/render.cs:296-300 (min(ceil(n/128), 500) + 4 iterations
+// of uvec4 per thread, 4 at a time: nodes of up to 64,512 points).
+__device__ __forceinline__ int64_t points_in_batch(int32_t num_points, int32_t first_point,
+                                                   int32_t quirks) {
     int64_t n = num_points;
+    if (quirks & CR_QUIRK_NODE_LOOP) {
+        if (n < 0) return 0;
+        const int64_t loop = min((n + 127) / 128, (int64_t)500);
+        const int64_t reach = 512 * ((loop + 4) / 4) - (first_point & 3);
+        return min(n, reach);
+    }
     if (quirks & CR_QUIRK_INCLUSIVE_END) n += 1;
     if (n > kPointsPerBatch) n = kPointsPerBatch;
     return n < 0 ? 0 : n;

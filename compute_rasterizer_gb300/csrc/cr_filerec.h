@@ -73,4 +73,23 @@ __host__ __device__ inline void file_record(const double* view, const double* pr
     mat_mul(fview, fworld, out->VW);
 }
 
+// compute_loop_nodes.h:128-139: the same uniforms as float products,
+// transform = (float(proj) * float(view)) * float(world), view * world in
+// float (CR_QUIRK_FLOAT_UNIFORMS).
+__host__ __device__ inline void file_record_float(const double* view, const double* proj,
+                                                  const double* box_min, FileRec* out) {
+    const double world[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0,
+                              box_min[0], box_min[1], box_min[2], 1};
+    float fv[16], fp[16], fw[16], pv[16];
+    for (int i = 0; i < 16; i++) {
+        fv[i] = (float)view[i];
+        fp[i] = (float)proj[i];
+        fw[i] = (float)world[i];
+    }
+    mat_mul(fp, fv, pv);
+    mat_mul(pv, fw, out->T);
+    frustum_planes(out->T, out->planes);
+    mat_mul(fv, fw, out->VW);
+}
+
 }  // namespace cr

@@ -63,6 +63,8 @@ struct ViewParams {
     int32_t lod_skip_level;  // >0: batches at level >= this are not rendered
     FileRec files[kInlineFiles];
     const FileRec* dfiles;   // nfiles records when nfiles > kInlineFiles, else null
+    float level4_px;         // level 4 below this projected size (100; loop_nodes 80)
+    int32_t one_world;       // every batch uses file 0's record (CR_QUIRK_ONE_WORLD)
 };
 
 // Scratch words at the head of the ctx scratch buffer.  The cull kernel sorts
@@ -105,7 +107,7 @@ struct BatchedLaunch {
 // matrices and the files' boxMin (host array, passed to the kernels in their
 // parameters, 1024 files per launch) into out[0, nfiles).
 int launch_file_records(const double view[16], const double proj[16], const double* box_min,
-                        int32_t nfiles, FileRec* out, void* stream);
+                        int32_t nfiles, FileRec* out, void* stream, int float_uniforms = 0);
 int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb_dispatch,
                 int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream);
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
@@ -113,12 +115,13 @@ int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int
 // variant 0: early-z, 1: dedup, 2: early-z & reduce (the three plain methods)
 int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
                  uint64_t* fb, int grid, int variant, void* stream);
+// tiles: CR_QUIRK_RESOLVE_TILES (image words outside full 16x16 tiles kept)
 int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgba,
                          int64_t rgba_words, uint32_t* image, int clear_after, uint64_t clear,
-                         void* stream);
+                         void* stream, int tiles = 0);
 int launch_resolve_color(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
                          uint64_t clear, void* stream);
-// tiles: CR_QUIRK_PLAIN_TILES; zero_rule: ucol == 0 resolves to opaque black
+// tiles: CR_QUIRK_RESOLVE_TILES; zero_rule: ucol == 0 resolves to opaque black
 // (early-z, early-z & reduce; not dedup)
 int launch_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,
                          uint64_t clear, int tiles, int zero_rule, void* stream);

@@ -45,7 +45,7 @@ namespace {
 constexpr int kFilesPerLaunch = 1024;
 struct FileChunk {
     double view[16], proj[16];
-    int32_t first, count;
+    int32_t first, count, float_uniforms;
     double box_min[3 * kFilesPerLaunch];
 };
 static_assert(sizeof(FileChunk) < 32000, "kernel parameters are limited to 32 KB");
@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(128) k_file_records(const __grid_constant__ Fi
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.count) return;
     FileRec r;
-    file_record(c.view, c.proj, &c.box_min[3 * i], &r);
+    if (c.float_uniforms) file_record_float(c.view, c.proj, &c.box_min[3 * i], &r);
+    else file_record(c.view, c.proj, &c.box_min[3 * i], &r);
     out[c.first + i] = r;
 }
 
@@ -87,9 +88,9 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
         int4 a = __ldg(r4), c = __ldg(r4 + 1), d = __ldg(r4 + 2);
         float mnx = __int_as_float(a.y), mny = __int_as_float(a.z), mnz = __int_as_float(a.w);
         float mxx = __int_as_float(c.x), mxy = __int_as_float(c.y), mxz = __int_as_float(c.z);
-        int32_t np = c.w, fp = d.x, fi = d.y;
-        int64_t count = points_in_batch(np, quirks);
-        bool ok = np >= 0 && np <= kPointsPerBatch && fp >= 0 &&
+        int32_t np = c.w, fp = d.x, fi = vp.one_world ? 0 : d.y;
+        int64_t count = points_in_batch(np, fp, quirks);
+        bool ok = np >= 0 && (np <= kPointsPerBatch || (quirks & CR_QUIRK_NODE_LOOP)) && fp >= 0 &&
                   (int64_t)fp + count + 4 <= capacity && fi >= 0 && fi < vp.nfiles;
         if (!ok) {
             atomicOr(&scratch[kErrWord], kErrBadBatch);
@@ -97,7 +98,8 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
             const FileRec& f = *file_rec(vp, fi);
             bool vis = !vp.culling || intersects_frustum(f.planes, mnx, mny, mnz, mxx, mxy, mxz);
             if (vis) {
-                int level = precision_level(vp.P, f.VW, vp.W, vp.H, mnx, mny, mnz, mxx, mxy, mxz);
+                int level = precision_level(vp.P, f.VW, vp.W, vp.H, mnx, mny, mnz, mxx, mxy, mxz,
+                                            vp.level4_px);
                 // compute_loop_nodes/render.cs:273-276: the level-of-detail cut
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
@@ -405,7 +407,8 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             const float mnx = __int_as_float(ra.y), mny = __int_as_float(ra.z), mnz = __int_as_float(ra.w);
             const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
             const int64_t first = rd.x;
-            const int32_t count = (int32_t)points_in_batch(rc.w, bl.quirks);
+            const int32_t count = (int32_t)points_in_batch(rc.w, rd.x, bl.quirks);
+            const int fi = vp.one_world ? 0 : rd.y;
             BatchCtx c;
             // render.cs:355-357, 392-394 boxSize / STEPS: a division by a power
             // of two is the same real value as the product with its exact
@@ -416,9 +419,9 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             c.sy = fmul(fsub(mxy, mny), inv);
             c.sz = fmul(fsub(mxz, mnz), inv);
             if constexpr (MANY) {
-                load_transform(vp.dfiles[rd.y].T, c);
+                load_transform(vp.dfiles[fi].T, c);
             } else {
-                const FileRec& f = vp.files[rd.y];
+                const FileRec& f = vp.files[fi];
                 load_transform(f.T, c);
             }
             c.Wf = (float)vp.W; c.Hf = (float)vp.H; c.W = vp.W;
@@ -521,14 +524,34 @@ __device__ __forceinline__ bool depth_valid(uint64_t v) {
     return d > 0.0f && d < 1000000.0f;
 }
 
-// resolve.cs:100-146 (index payload) -- 2 pixels per thread.
+// Whether pixel p lies in the floor(W/16) x floor(H/16) tiles a resolve of
+// 16x16 groups covers (CR_QUIRK_RESOLVE_TILES).
+__device__ __forceinline__ bool in_tiles(int64_t p, int32_t W, int32_t H) {
+    const int64_t y = p / W, x = p - y * W;
+    return x < (W & ~15) && y < (H & ~15);
+}
+
+// resolve.cs:100-146 (index payload) -- 2 pixels per thread.  tiles: only the
+// pixels of full 16x16 tiles are resolved (compute_loop_nodes.h:199-201); the
+// re-clear covers every pixel (loop_nodes clears separately,
+// compute_loop_nodes.h:239-251).
 __global__ void k_resolve_index(int64_t P, int64_t tail, uint64_t* __restrict__ fb,
                                 const uint32_t* __restrict__ rgba, int64_t rgba_words,
-                                uint32_t* __restrict__ image, int clear_after, uint64_t clear) {
+                                uint32_t* __restrict__ image, int clear_after, uint64_t clear,
+                                int32_t W, int32_t H, int tiles) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t p = 2 * t;
     if (p < P) {
-        if (p + 1 < P) {
+        if (tiles) {
+            for (int64_t q = p; q < p + 2 && q < P; q++) {
+                if (in_tiles(q, W, H)) {
+                    const uint64_t v = fb[q];
+                    const uint32_t i0 = depth_valid(v) ? (uint32_t)v : 0u;
+                    image[q] = (i0 == 0u || i0 >= rgba_words) ? kBackground : __ldg(rgba + i0);
+                }
+                if (clear_after) fb[q] = clear;
+            }
+        } else if (p + 1 < P) {
             ulonglong2 v = reinterpret_cast<const ulonglong2*>(fb)[t];
             uint32_t i0 = depth_valid(v.x) ? (uint32_t)v.x : 0u;
             uint32_t i1 = depth_valid(v.y) ? (uint32_t)v.y : 0u;
@@ -579,7 +602,7 @@ __device__ __forceinline__ uint32_t plain_rgba8(uint64_t v, int zero_rule) {
     return ucol == 0u && zero_rule ? 0xFF000000u : ucol;
 }
 
-// tiles != 0 (CR_QUIRK_PLAIN_TILES): only the pixels of the floor(W/16) x
+// tiles != 0 (CR_QUIRK_RESOLVE_TILES): only the pixels of the floor(W/16) x
 // floor(H/16) tiles of 16x16 that the reference dispatches
 // (compute_2021_earlyz.h:161-163) are resolved and re-cleared; every other
 // image and framebuffer word, the guard tail included, keeps its value.
@@ -656,10 +679,11 @@ inline int blocks_for(int64_t n, int per) { return (int)((n + per - 1) / per); }
 }  // namespace
 
 int launch_file_records(const double view[16], const double proj[16], const double* box_min,
-                        int32_t nfiles, FileRec* out, void* stream) {
+                        int32_t nfiles, FileRec* out, void* stream, int float_uniforms) {
     // the chunk travels by value in the kernel parameters: no staging buffer
     // whose lifetime would have to outlast the launch
-    static thread_local FileChunk c;
+    FileChunk c;
+    c.float_uniforms = float_uniforms;
     for (int i = 0; i < 16; i++) {
         c.view[i] = view[i];
         c.proj[i] = proj[i];
@@ -786,11 +810,11 @@ int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, in
 
 int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgba,
                          int64_t rgba_words, uint32_t* image, int clear_after, uint64_t clear,
-                         void* stream) {
+                         void* stream, int tiles) {
     int64_t P = (int64_t)W * H, tail = (int64_t)W + 1;
     int64_t threads = (P + 1) / 2 > tail ? (P + 1) / 2 : tail;
     return launch_k(k_resolve_index, blocks_for(threads, 256), 256, (cudaStream_t)stream, P, tail,
-                    fb, rgba, rgba_words, image, clear_after, clear);
+                    fb, rgba, rgba_words, image, clear_after, clear, W, H, tiles);
 }
 
 int launch_resolve_color(int32_t W, int32_t H, uint64_t* fb, uint32_t* image, int clear_after,

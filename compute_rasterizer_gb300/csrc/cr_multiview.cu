@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_mv_cull(const MVView* __restrict__ view
         const float mnx = __int_as_float(a.y), mny = __int_as_float(a.z), mnz = __int_as_float(a.w);
         const float mxx = __int_as_float(c.x), mxy = __int_as_float(c.y), mxz = __int_as_float(c.z);
         const int32_t np = c.w, fp = d.x, fi = d.y;
-        const int64_t count = points_in_batch(np, quirks);
+        const int64_t count = points_in_batch(np, fp, quirks);
         const bool ok = np >= 0 && np <= kPointsPerBatch && fp >= 0 &&
                         (int64_t)fp + count + 4 <= capacity && fi >= 0 && fi < nfiles;
         if (!ok) {
@@ -255,7 +255,7 @@ __device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
         const float mnx = __int_as_float(ra.y), mny = __int_as_float(ra.z), mnz = __int_as_float(ra.w);
         const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
         const int64_t first = rd.x;
-        const int32_t count = (int32_t)points_in_batch(rc.w, a.quirks);
+        const int32_t count = (int32_t)points_in_batch(rc.w, rd.x, a.quirks);
         const int fi = rd.y;
         // the group's visible views into shared memory
         for (int t = threadIdx.x; t < a.G * kSlotWords; t += BLOCK) {

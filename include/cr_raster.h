@@ -54,14 +54,16 @@ typedef enum cr_status {
 
 /* Method ids; names as registered by the reference (compute_loop_las.h:82,
  * compute_loop_las2.h:82, compute_loop_las_hqs.h:88, compute_2021_earlyz.h:52,
- * compute_2021_dedup.h:52, compute_2021_earlyz_reduce.h:52). */
+ * compute_2021_dedup.h:52, compute_2021_earlyz_reduce.h:52,
+ * compute_loop_nodes.h:76). */
 typedef enum cr_method {
     CR_METHOD_LOOP_LAS = 0,          /* "loop_las" */
     CR_METHOD_LOOP_LAS_PREFETCH = 1, /* "loop_las_prefetch" */
     CR_METHOD_LOOP_LAS_HQS = 2,      /* "loop_las_hqs" */
     CR_METHOD_EARLYZ = 3,            /* "(2021) early-z" */
     CR_METHOD_DEDUP = 4,             /* "(2021) dedup" */
-    CR_METHOD_EARLYZ_REDUCE = 5      /* "(2021) early-z & reduce" */
+    CR_METHOD_EARLYZ_REDUCE = 5,     /* "(2021) early-z & reduce" */
+    CR_METHOD_LOOP_NODES = 6         /* "loop_nodes": Potree octree nodes as batches (cr_potree.h) */
 } cr_method;
 
 typedef enum cr_payload {
@@ -80,10 +82,24 @@ typedef enum cr_quirk {
      * l with (l + r) % 512 < 4 are skipped, and the last r points (l >= 10240 - r) are never
      * visited.  Batched single-view, multi-view and server paths. */
     CR_QUIRK_UVEC4_BASE = 8,
-    /* The 2021 methods' resolve dispatches floor(W/16) x floor(H/16) groups of 16x16
-     * (compute_2021_earlyz.h:161-163): pixels outside those tiles are neither resolved nor
-     * re-cleared; their image and framebuffer words keep their values. */
-    CR_QUIRK_PLAIN_TILES = 16
+    /* The resolve dispatches floor(W/16) x floor(H/16) groups of 16x16
+     * (compute_2021_earlyz.h:161-163, compute_loop_nodes.h:199-201): pixels outside those
+     * tiles keep their image words.  The 2021 methods re-clear in the resolve, so their
+     * framebuffer words there keep their values too; loop_nodes clears its framebuffer
+     * separately (compute_loop_nodes.h:239-251), every pixel. */
+    CR_QUIRK_RESOLVE_TILES = 16,
+    /* compute_loop_nodes/render.cs:296-300: a batch (an octree node) visits
+     * min(numPoints, 512 * floor((min(ceil(numPoints / 128), 500) + 4) / 4) - firstPoint % 4)
+     * points, so nodes hold up to 64,512 points, with no 10,240-point cap. */
+    CR_QUIRK_NODE_LOOP = 32,
+    /* compute_loop_nodes/render.cs:199: precision level 4 below 80 pixels (loop_las: 100). */
+    CR_QUIRK_LEVEL4_80PX = 64,
+    /* every batch rendered with file 0's world: Potree batches carry the node level in the
+     * file_index slot (PotreeData.h:335-350), and loop_nodes has one world matrix. */
+    CR_QUIRK_ONE_WORLD = 128,
+    /* uniforms as float products: transform = float(proj) * float(view) * world
+     * (compute_loop_nodes.h:128-139; loop_las forms them in double and casts). */
+    CR_QUIRK_FLOAT_UNIFORMS = 256
 } cr_quirk;
 
 #define CR_QUIRKS_METHOD_DEFAULT (-1)
@@ -125,8 +141,9 @@ typedef struct cr_render_params {
     int32_t ctas_per_sm;     /* persistent CTAs per SM; 0 = tuned default */
     int32_t views_per_group; /* multi-view: views sharing one point fetch; 0 = tuned default */
     int32_t lod_skip_level;  /* >0: skip batches whose precision level is >= this, the level-of-
-                                detail cut of compute_loop_nodes/render.cs:273-276 (which uses 4);
-                                0 = render every visible batch, as the loop_las methods do */
+                                detail cut of compute_loop_nodes/render.cs:273-276 (loop_nodes'
+                                default: 4); 0 = render every visible batch, as the loop_las
+                                methods do */
     int32_t reserved[4];
 } cr_render_params;
 

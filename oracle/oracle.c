@@ -197,6 +197,23 @@ void or_file_setup(const double view[16], const double proj[16], const double bo
     or_mat4f_mul(fview, fworld, out->view_world);
 }
 
+/* compute_loop_nodes.h:128-139: mat4 view, proj (float casts of the double
+ * matrices), worldViewProj = proj * view * world in float. */
+void or_file_setup_float(const double view[16], const double proj[16], const double box_min[3],
+                         or_file_frame* out) {
+    double world[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, box_min[0], box_min[1], box_min[2], 1};
+    float fv[16], fp[16], fw[16], pv[16];
+    for (int i = 0; i < 16; i++) {
+        fv[i] = (float)view[i];
+        fp[i] = (float)proj[i];
+        fw[i] = (float)world[i];
+    }
+    or_mat4f_mul(fp, fv, pv);
+    or_mat4f_mul(pv, fw, out->transform);
+    or_frustum_planes(out->transform, out->planes);
+    or_mat4f_mul(fv, fw, out->view_world);
+}
+
 void or_proj_float(const double proj[16], float out[16]) {
     for (int i = 0; i < 16; i++) out[i] = (float)proj[i];
 }
@@ -248,7 +265,7 @@ int or_precision_level(const or_frame* fr, const or_file_frame* file, const floa
     float sex = (W * (pex + 1.0f)) / 2.0f, sey = (H * (pey + 1.0f)) / 2.0f;
     float ex = sex - scx, ey = sey - scy;
     float px = sqrtf(ex * ex + ey * ey);
-    if (px < 100.0f) return 4;
+    if (px < ((fr->quirks & OR_QUIRK_LEVEL4_80PX) ? 80.0f : 100.0f)) return 4;
     if (px < 200.0f) return 3;
     if (px < 500.0f) return 2;
     if (px < 10000.0f) return 1;
@@ -328,6 +345,16 @@ static int project(const float T[16], int32_t W, int32_t H, const float p[3], in
  * by the 80 x 128 loop (Resources.h:4-6). */
 int64_t or_points_in_batch(const or_batch* b, int32_t quirks) {
     int64_t n = b->num_points;
+    if (quirks & OR_QUIRK_NODE_LOOP) {
+        /* compute_loop_nodes/render.cs:296-300: loopSize = min(ceil(n / 128), 500)
+         * + 4; i < loopSize / 4 iterations of one uvec4 per thread from
+         * firstPoint / 4; `localIndex >= numPoints` skips (continue) */
+        if (n < 0) return 0;
+        int64_t loop = (n + 127) / 128;
+        if (loop > 500) loop = 500;
+        int64_t reach = 512 * ((loop + 4) / 4) - (b->first_point & 3);
+        return n < reach ? n : reach;
+    }
     if (quirks & OR_QUIRK_INCLUSIVE_END) n = n + 1;
     if (n > POINTS_PER_BATCH) n = POINTS_PER_BATCH;
     if (n < 0) n = 0;
@@ -372,7 +399,7 @@ static void raster_range(const raster_job* j) {
     const or_frame* fr = j->fr;
     for (int64_t bi = j->b0; bi < j->b1; bi++) {
         const or_batch* b = &j->batches[bi];
-        const or_file_frame* file = &fr->files[b->file_index];
+        const or_file_frame* file = &fr->files[(fr->quirks & OR_QUIRK_ONE_WORLD) ? 0 : b->file_index];
         float wmin[3] = {b->min_x, b->min_y, b->min_z};
         float wmax[3] = {b->max_x, b->max_y, b->max_z};
         if (fr->frustum_culling && !or_intersects_frustum(file->planes, wmin, wmax)) continue;
@@ -446,6 +473,19 @@ void or_resolve_index(int32_t W, int32_t H, const uint64_t* fb, const uint32_t* 
     }
 }
 
+void or_resolve_index_tiles(int32_t W, int32_t H, const uint64_t* fb, const uint32_t* rgba,
+                            uint32_t* out) {
+    for (int32_t y = 0; y < H / 16 * 16; y++)
+        for (int32_t x = 0; x < W / 16 * 16; x++) {
+            const int64_t p = (int64_t)x + (int64_t)y * W;
+            uint64_t v = fb[p];
+            float depth = u2f((uint32_t)(v >> 32));
+            uint32_t id = 0;
+            if (depth > 0.0f && depth < 1000000.0f) id = (uint32_t)v;
+            out[p] = id == 0 ? 0x00443322u : rgba[id];
+        }
+}
+
 void or_resolve_color(int32_t W, int32_t H, const uint64_t* fb, uint32_t* out) {
     int64_t P = (int64_t)W * H;
     for (int64_t p = 0; p < P; p++) {
@@ -470,7 +510,7 @@ void or_hqs_depth(const or_frame* fr, const or_batch* batches, int64_t num_batch
     int64_t nb = or_dispatch_batches(num_batches, num_points, fr->quirks);
     for (int64_t bi = 0; bi < nb; bi++) {
         const or_batch* b = &batches[bi];
-        const or_file_frame* file = &fr->files[b->file_index];
+        const or_file_frame* file = &fr->files[(fr->quirks & OR_QUIRK_ONE_WORLD) ? 0 : b->file_index];
         float wmin[3] = {b->min_x, b->min_y, b->min_z};
         float wmax[3] = {b->max_x, b->max_y, b->max_z};
         if (fr->frustum_culling && !or_intersects_frustum(file->planes, wmin, wmax)) continue;
@@ -500,7 +540,7 @@ void or_hqs_color(const or_frame* fr, const or_batch* batches, int64_t num_batch
     int64_t nb = or_dispatch_batches(num_batches, num_points, fr->quirks);
     for (int64_t bi = 0; bi < nb; bi++) {
         const or_batch* b = &batches[bi];
-        const or_file_frame* file = &fr->files[b->file_index];
+        const or_file_frame* file = &fr->files[(fr->quirks & OR_QUIRK_ONE_WORLD) ? 0 : b->file_index];
         float wmin[3] = {b->min_x, b->min_y, b->min_z};
         float wmax[3] = {b->max_x, b->max_y, b->max_z};
         if (fr->frustum_culling && !or_intersects_frustum(file->planes, wmin, wmax)) continue;
@@ -634,12 +674,12 @@ void or_raster_plain_warp(const float T[16], int32_t W, int32_t H, const or_vert
 /* compute_2021_earlyz/resolve.cs:41-77, compute_2021_dedup/resolve.cs:15-42,
  * compute_2021_earlyz_reduce/resolve.cs:41-77.  The reference dispatches
  * floor(W/16) x floor(H/16) groups of 16 x 16 threads (compute_2021_earlyz.h:
- * 161-163), so with OR_QUIRK_PLAIN_TILES the pixels past the last full tile
+ * 161-163), so with OR_QUIRK_RESOLVE_TILES the pixels past the last full tile
  * keep their image and framebuffer words.  Without it every pixel is resolved
  * and the framebuffer's guard tail (W + 1 words past W*H) is re-cleared too. */
 void or_resolve_plain(int32_t W, int32_t H, uint64_t* fb, uint8_t* out, uint64_t reclear,
                       int32_t quirks, int32_t zero_rule) {
-    const int tiles = (quirks & OR_QUIRK_PLAIN_TILES) != 0;
+    const int tiles = (quirks & OR_QUIRK_RESOLVE_TILES) != 0;
     const int32_t Wt = tiles ? W / 16 * 16 : W, Ht = tiles ? H / 16 * 16 : H;
     for (int32_t y = 0; y < Ht; y++) {
         for (int32_t x = 0; x < Wt; x++) {

@@ -75,7 +75,10 @@ enum {
     OR_QUIRK_INCLUSIVE_END = 2, /* H2: `localIndex > numPoints` bound (las2/render.cs:341, hqs/depth.cs:276) */
     OR_QUIRK_DISPATCH_BY_POINTS = 4, /* H3: dispatch ceil(numPoints/10240) batch records (compute_loop_las2.h:234) */
     OR_QUIRK_UVEC4_BASE = 8,  /* H6: las2's uvec4 addressing from firstPoint/4 (las2/render.cs:319-341) */
-    OR_QUIRK_PLAIN_TILES = 16 /* the 2021 resolves cover floor(W/16) x floor(H/16) tiles (compute_2021_earlyz.h:161-163) */
+    OR_QUIRK_RESOLVE_TILES = 16, /* resolves cover floor(W/16) x floor(H/16) tiles (compute_2021_earlyz.h:161-163) */
+    OR_QUIRK_NODE_LOOP = 32,     /* loop_nodes' per-node loop (compute_loop_nodes/render.cs:296-300) */
+    OR_QUIRK_LEVEL4_80PX = 64,   /* level 4 below 80 px (compute_loop_nodes/render.cs:199) */
+    OR_QUIRK_ONE_WORLD = 128     /* every batch uses file 0 (Potree batches hold the level there) */
 };
 
 enum { OR_PAYLOAD_INDEX = 0, OR_PAYLOAD_COLOR = 1 };
@@ -102,6 +105,9 @@ void or_orbit_world(double yaw, double pitch, double radius, const double target
 void or_frustum_planes(const float m[16], float planes[6][4]);
 void or_file_setup(const double view[16], const double proj[16], const double box_min[3],
                    or_file_frame* out);
+/* compute_loop_nodes.h:128-139: the uniforms as float matrix products */
+void or_file_setup_float(const double view[16], const double proj[16], const double box_min[3],
+                         or_file_frame* out);
 void or_proj_float(const double proj[16], float out[16]);
 
 /* ---- per-batch culling and precision level (A4, A5) ----------------------- */
@@ -122,6 +128,10 @@ void or_raster_batched_mt(const or_frame* fr, const or_batch* batches, int64_t n
 /* resolve.cs:100-193 (window 0): index payload -> ssRGBA gather, 0 -> background */
 void or_resolve_index(int32_t width, int32_t height, const uint64_t* fb, const uint32_t* rgba,
                       uint32_t* out);
+/* the same over the floor(W/16) x floor(H/16) tiles only (compute_loop_nodes.h:199-201):
+ * other pixels of `out` keep their values */
+void or_resolve_index_tiles(int32_t width, int32_t height, const uint64_t* fb,
+                            const uint32_t* rgba, uint32_t* out);
 /* color payload: the low word is already the color */
 void or_resolve_color(int32_t width, int32_t height, const uint64_t* fb, uint32_t* out);
 void or_fill_u64(uint64_t* buf, int64_t n, uint64_t value);
@@ -144,7 +154,7 @@ void or_raster_plain(const float transform[16], int32_t width, int32_t height,
  * warp reductions over 32 consecutive points, key depth << 24 | color. */
 void or_raster_plain_warp(const float T[16], int32_t W, int32_t H, const or_vertex* v, int64_t n,
                           uint64_t* fb, int32_t variant);
-/* quirks: OR_QUIRK_PLAIN_TILES; zero_rule: ucol == 0 resolves to (0,0,0,255)
+/* quirks: OR_QUIRK_RESOLVE_TILES; zero_rule: ucol == 0 resolves to (0,0,0,255)
  * (early-z and early-z & reduce; the dedup resolve has no such rule). */
 void or_resolve_plain(int32_t width, int32_t height, uint64_t* fb, uint8_t* out_rgba8,
                       uint64_t reclear, int32_t quirks, int32_t zero_rule);

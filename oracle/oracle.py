@@ -15,7 +15,8 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 GLMREF = HERE / "_ref" / "libglmref.so"
 
-L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS, UVEC4_BASE, PLAIN_TILES = 1, 2, 4, 8, 16
+L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS, UVEC4_BASE, RESOLVE_TILES = 1, 2, 4, 8, 16
+NODE_LOOP, LEVEL4_80PX, ONE_WORLD = 32, 64, 128
 PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
 
 
@@ -58,6 +59,8 @@ def lib() -> C.CDLL:
         P, I64, I32 = C.c_void_p, C.c_int64, C.c_int32
         sig = {
             "or_file_setup": [P, P, P, C.POINTER(FileFrame)],
+            "or_file_setup_float": [P, P, P, C.POINTER(FileFrame)],
+            "or_resolve_index_tiles": [I32, I32, P, P, P],
             "or_proj_float": [P, P],
             "or_raster_batched": [C.POINTER(Frame), P, I64, I64, P, P, P, P, P],
             "or_raster_batched_mt": [C.POINTER(Frame), P, I64, I64, P, P, P, P, P, C.c_int],
@@ -118,16 +121,19 @@ def fnv(a: np.ndarray) -> int:
     return int(lib().or_fnv1a64(_p(a), a.nbytes))
 
 
-def make_frame(view, proj, width, height, box_mins, culling=1, quirks=0, payload=0, lod_skip_level=0):
-    """Frame + per-file records from double matrices (compute_loop_las.h:141-200)."""
+def make_frame(view, proj, width, height, box_mins, culling=1, quirks=0, payload=0, lod_skip_level=0,
+               float_uniforms=False):
+    """Frame + per-file records from double matrices (compute_loop_las.h:141-200;
+    float_uniforms: the float products of compute_loop_nodes.h:128-139)."""
     o = lib()
     view = np.ascontiguousarray(view, np.float64).reshape(16)
     proj = np.ascontiguousarray(proj, np.float64).reshape(16)
     box_mins = np.ascontiguousarray(box_mins, np.float64).reshape(-1, 3)
     files = (FileFrame * len(box_mins))()
+    setup = o.or_file_setup_float if float_uniforms else o.or_file_setup
     for i, bm in enumerate(box_mins):
         bm = np.ascontiguousarray(bm)
-        o.or_file_setup(_p(view), _p(proj), _p(bm), C.byref(files[i]))
+        setup(_p(view), _p(proj), _p(bm), C.byref(files[i]))
     fr = Frame()
     o.or_proj_float(_p(proj), C.cast(fr.proj, C.c_void_p))
     fr.width, fr.height = int(width), int(height)
@@ -175,6 +181,15 @@ def resolve_index(width, height, fb, rgba) -> np.ndarray:
     return out
 
 
+def resolve_index_tiles(width, height, fb, rgba, image=None) -> np.ndarray:
+    """resolve_index over full 16x16 tiles only; other pixels keep `image`'s
+    words (zeros by default)."""
+    out = np.zeros(width * height, np.uint32) if image is None else np.array(image, np.uint32)
+    r = pad_stream(rgba)
+    lib().or_resolve_index_tiles(width, height, _p(fb), _p(r), _p(out))
+    return out
+
+
 def resolve_color(width, height, fb) -> np.ndarray:
     out = np.empty(width * height, dtype=np.uint32)
     lib().or_resolve_color(width, height, _p(fb), _p(out))
@@ -195,9 +210,9 @@ def hqs(frame, batches, n, low, med, hig, rgba):
 
 
 def plain(view, proj, width, height, vertices, clear=0xFFFFFFFFFFFFFFFF,
-          reclear=0xFFFFFFFFFF3C321E, variant=0, quirks=PLAIN_TILES, fb=None, image=None):
+          reclear=0xFFFFFFFFFF3C321E, variant=0, quirks=RESOLVE_TILES, fb=None, image=None):
     """The plain 16 B path: variant 0 early-z, 1 dedup, 2 early-z & reduce.
-    quirks: PLAIN_TILES (the methods' default) or 0.  `fb` / `image`: the
+    quirks: RESOLVE_TILES (the methods' default) or 0.  `fb` / `image`: the
     previous frame's framebuffer and image (pixels outside the resolved tiles
     keep them); a fresh fb filled with `clear` and a zero image by default.
     Returns (fb after the raster, image, fb after the resolve)."""

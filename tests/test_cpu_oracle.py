@@ -396,7 +396,7 @@ def test_plain_resolve_tiles():
         rng.integers(1, 2**24, w * h + w + 1, dtype=np.uint64)
     img0 = rng.integers(0, 2**32, w * h, dtype=np.uint64).astype(np.uint32)
     img, f = img0.copy(), fb.copy()
-    O.lib().or_resolve_plain(w, h, f.ctypes.data, img.ctypes.data, 7, O.PLAIN_TILES, 1)
+    O.lib().or_resolve_plain(w, h, f.ctypes.data, img.ctypes.data, 7, O.RESOLVE_TILES, 1)
     x, y = np.meshgrid(np.arange(w), np.arange(h))
     inside = ((x < 32) & (y < 32)).reshape(-1)
     ucol = (fb[: w * h] & np.uint64(0xFFFFFF)).astype(np.uint32)

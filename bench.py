@@ -130,12 +130,15 @@ def cpu_sample(points_full: int, extent_full: float, seed: int, sample: int):
 
 
 def encode_parallel(rec, n, hdr, threads=None):
-    """cr_encode_las over batch-aligned chunks on host threads (ctypes drops the GIL)."""
+    """The oracle's loadLas restatement (or_encode_las) over batch-aligned
+    chunks on host threads (ctypes drops the GIL): the CPU legs encode with the
+    oracle, not with the product's host encoder."""
     import concurrent.futures as cf
 
     from compute_rasterizer_gb300 import _lib as L
-    lib = L.load()
-    nb = int(lib.cr_num_batches(n))
+    from oracle import oracle as O
+    lib = O.lib()
+    nb = -(-n // 10240)
     batches = np.zeros(nb, L.BATCH_DTYPE)
     st = [np.zeros(n, np.uint32) for _ in range(4)]
     sc, of, mn = (np.ascontiguousarray(x[:], np.float64) for x in (hdr.scale, hdr.offset, hdr.min))
@@ -147,10 +150,10 @@ def encode_parallel(rec, n, hdr, threads=None):
         if b0 >= b1:
             return 0
         p0, p1 = b0 * 10240, min(n, b1 * 10240)
-        return lib.cr_encode_las(rec.ctypes.data + p0 * 26, p1 - p0, 26, 2, sc.ctypes.data,
-                                 of.ctypes.data, mn.ctypes.data, p0, 0,
-                                 batches.ctypes.data + b0 * 64,
-                                 *(s.ctypes.data + p0 * 4 for s in st))
+        lib.or_encode_las(rec.ctypes.data + p0 * 26, p1 - p0, 26, 2, sc.ctypes.data,
+                          of.ctypes.data, mn.ctypes.data, p0, 0, batches.ctypes.data + b0 * 64,
+                          *(s.ctypes.data + p0 * 4 for s in st))
+        return 0
     with cf.ThreadPoolExecutor(threads) as ex:
         assert all(r == 0 for r in ex.map(job, range(threads)))
     return (batches, *st)

@@ -14,6 +14,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 GLMREF = HERE / "_ref" / "libglmref.so"
+SFREF = HERE / "_ref" / "libsfref.so"
 
 L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS, UVEC4_BASE, RESOLVE_TILES = 1, 2, 4, 8, 16
 NODE_LOOP, LEVEL4_80PX, ONE_WORLD = 32, 64, 128
@@ -113,6 +114,14 @@ def glmref() -> C.CDLL:
     for k, v in sig.items():
         getattr(g, k).argtypes = v
         getattr(g, k).restype = None
+    return g
+
+
+def sfref() -> C.CDLL:
+    """The Sort_Frugal probe built from the reference's sorter (oracle/_ref)."""
+    g = C.CDLL(str(SFREF))
+    g.sfref_morton.argtypes = [C.c_uint32] * 3
+    g.sfref_morton.restype = C.c_uint64
     return g
 
 

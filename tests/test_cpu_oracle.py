@@ -151,6 +151,32 @@ def test_generator_deterministic_and_morton_sorted():
     assert hs.min[0] == xyz[:, 0].min() * 0.001 and hs.max[2] == xyz[:, 2].max() * 0.001
 
 
+@pytest.mark.skipif(not O.SFREF.exists(), reason="Sort_Frugal probe not built (no reference tree)")
+def test_morton_order_matches_reference_sorter():
+    """The oracle's Morton code equals Sort_Frugal's mortonEncode_magicbits on
+    full 32-bit inputs (both keep 21 bits), and the product's host sort leaves
+    records in nondecreasing reference code over the reference's quantisation,
+    apart from the far-face value 2^21 that the product clamps to 2^21 - 1."""
+    sf, o = O.sfref(), O.lib()
+    rng = np.random.default_rng(5)
+    vals = np.concatenate([rng.integers(0, 2**32, (3000, 3), dtype=np.uint64),
+                           rng.integers(0, 2**21, (3000, 3), dtype=np.uint64),
+                           np.array([[0, 0, 0], [2**21 - 1] * 3, [2**21] * 3, [2**32 - 1] * 3],
+                                    np.uint64)])
+    for x, y, z in vals.tolist():
+        assert o.or_morton3(x, y, z) == sf.sfref_morton(x, y, z)
+    p = synth.synth_params(L.SYNTH_TERRAIN_BOXES, 300.0, 4, num_boxes=4, points_per_box=800)
+    s, hs = synth.las_records_host(p, 30000, morton=True)
+    xyz = np.frombuffer(s.reshape(-1, 26)[:, :12].tobytes(), "<i4").reshape(-1, 3)
+    mn = np.array(hs.min[:])
+    cube = max(hs.max[k] - hs.min[k] for k in range(3))
+    pts = xyz * np.array(hs.scale[:]) + np.array(hs.offset[:])
+    q = ((pts - mn) / cube * 2097152.0).astype(np.uint64)
+    q = np.minimum(q, 2**21 - 1)
+    codes = [sf.sfref_morton(int(x), int(y), int(z)) for x, y, z in q.tolist()]
+    assert all(codes[i] <= codes[i + 1] for i in range(len(codes) - 1))
+
+
 def test_quirk_semantics():
     cl = encoded(n=25000, extent=150.0, seed=3)
     cam = cameras(cl)["near"]

@@ -17,7 +17,7 @@ POINTS_PER_BATCH = 10240
 
 # cr_status
 OK, INVALID_ARG, OUT_OF_MEMORY, ADMISSION_REJECTED, TIMEOUT, CUDA_ERROR, DEVICE_FLAG, \
-    UNSUPPORTED, NOT_FOUND = range(9)
+    UNSUPPORTED, NOT_FOUND, CORRUPT = range(10)
 
 # methods / payloads / quirks / streams / fb kinds
 METHOD_LOOP_LAS, METHOD_LOOP_LAS_PREFETCH, METHOD_LOOP_LAS_HQS, METHOD_EARLYZ, METHOD_DEDUP, \
@@ -137,6 +137,20 @@ class LasInfo(C.Structure):
                 ("min", C.c_double * 3), ("max", C.c_double * 3)]
 
 
+LAZ_MAX_ITEMS = 8
+LAZ_ITEM_BYTE, LAZ_ITEM_POINT10, LAZ_ITEM_GPSTIME11, LAZ_ITEM_RGB12 = 0, 6, 7, 8
+LAZ_POINTWISE, LAZ_POINTWISE_CHUNKED = 1, 2
+LAZ_DEFAULT_CHUNK, LAZ_VARIABLE_CHUNKS = 50000, -1
+
+
+class LazInfo(C.Structure):
+    _fields_ = [("las", LasInfo), ("compressor", C.c_int32), ("num_items", C.c_int32),
+                ("item_type", C.c_int32 * LAZ_MAX_ITEMS), ("item_size", C.c_int32 * LAZ_MAX_ITEMS),
+                ("item_version", C.c_int32 * LAZ_MAX_ITEMS),
+                ("version_major", C.c_int32), ("version_minor", C.c_int32),
+                ("chunk_size", C.c_int64), ("num_chunks", C.c_int64), ("points_at", C.c_int64)]
+
+
 LAS_MIN_HEADER, LAS_14_HEADER = 227, 375
 MAX_POINTS_PER_LOAD = 1024000
 
@@ -225,6 +239,14 @@ _SIGS = {
     "cr_potree_load": (I32, [P, P, I32, PP, P]),
     "cr_cloud_load_las": (I32, [P, P, P, I64, C.POINTER(LasInfo), I64, I64, I32, P]),
     "cr_las_num_batches": (I64, [I64]),
+    # cr_laz.h
+    "cr_laz_open": (I32, [P, I64, PP, C.POINTER(LazInfo)]),
+    "cr_laz_close": (I32, [P]),
+    "cr_laz_decode": (I32, [P, I64, I64, P, I32]),
+    "cr_cloud_load_laz": (I32, [P, P, P, I64, I64, I32, I32, P]),
+    "cr_laz_vlr": (I32, [I32, I32, I64, P, I64, C.POINTER(I64)]),
+    "cr_laz_compress": (I32, [P, I64, I32, I32, I64, I64, I64, P, I64, C.POINTER(I64), I32]),
+    "cr_laz_compress_bound": (I64, [I64, I32, I64]),
     # cr_serve.h
     "cr_server_create": (I32, [P, C.POINTER(ServerConfig), PP]),
     "cr_server_destroy": (I32, [P]),

@@ -18,7 +18,7 @@ LIB = OUT / "libcr_raster.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 SOURCES = ["cr_api.cpp", "cr_kernels.cu", "cr_synth.cu", "cr_noalloc.cu", "cr_multiview.cu", "cr_serve.cpp",
-           "cr_las.cpp", "cr_potree.cpp"]
+           "cr_las.cpp", "cr_potree.cpp", "cr_laz.cpp"]
 
 # -fmad=false: no implicit contraction; explicit __fmaf_rn only.
 NVCC_FLAGS = [
@@ -60,7 +60,7 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
     tmp = LIB.with_suffix(".so.tmp")
     cudalib = Path(nvcc()).resolve().parent.parent / "lib64"
-    cmd = [nvcc(), ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart",
+    cmd = [nvcc(), ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lpthread",
            "-Xlinker", "-rpath", "-Xlinker", str(cudalib)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

@@ -275,6 +275,7 @@ const char* cr_status_string(cr_status s) {
         case CR_ERR_DEVICE_FLAG: return "device error flag raised";
         case CR_ERR_UNSUPPORTED: return "unsupported";
         case CR_ERR_NOT_FOUND: return "not found";
+        case CR_ERR_CORRUPT: return "corrupt data";
     }
     return "unknown status";
 }

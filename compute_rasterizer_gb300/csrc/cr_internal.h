@@ -158,6 +158,16 @@ bool cloud_info(const cr_cloud* cloud, CloudInfo* out);
 int default_quirks_for(int32_t method);
 // cr_ctx_check(NULL, stream): the no-alloc array's error flag (cr_noalloc.cu)
 cr_status noalloc_check(void* stream);
+
+// k_encode over device records with the RGB triple at byte `rgb_offset` of a
+// record, or colour 0 for rgb_offset < 0 (LAZ records without RGB, whose
+// zeroed rgb loadLaz encodes); cr_encode_las_device derives the offset from
+// the point format.
+cr_status encode_records_device(const uint8_t* d_rec, int64_t n, int32_t bpp, int32_t rgb_offset,
+                                const double scale[3], const double offset[3], const double box_min[3],
+                                int64_t sparse_offset, int32_t file_index, cr_batch* d_batches,
+                                uint32_t* d_lo, uint32_t* d_md, uint32_t* d_hi, uint32_t* d_rgba,
+                                void* stream);
 int ctx_device(const cr_ctx* ctx);
 
 // ---- multi-view frames (cr_multiview.cu), shared by cr_mv plans and the server

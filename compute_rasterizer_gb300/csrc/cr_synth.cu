@@ -429,11 +429,15 @@ __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __r
         lo[pi] = ((q[0] >> 20) & 1023u) | (((q[1] >> 20) & 1023u) << 10) | (((q[2] >> 20) & 1023u) << 20);
         md[pi] = ((q[0] >> 10) & 1023u) | (((q[1] >> 10) & 1023u) << 10) | (((q[2] >> 10) & 1023u) << 20);
         hi[pi] = (q[0] & 1023u) | ((q[1] & 1023u) << 10) | ((q[2] & 1023u) << 20);
-        uint32_t R = get_u16(r + a.rgb), G = get_u16(r + a.rgb + 2), B = get_u16(r + a.rgb + 4);
-        R = R < 256u ? R : R / 256u;
-        G = G < 256u ? G : G / 256u;
-        B = B < 256u ? B : B / 256u;
-        rgba[pi] = R | (G << 8) | (B << 16);
+        if (a.rgb >= 0) {
+            uint32_t R = get_u16(r + a.rgb), G = get_u16(r + a.rgb + 2), B = get_u16(r + a.rgb + 4);
+            R = R < 256u ? R : R / 256u;
+            G = G < 256u ? G : G / 256u;
+            B = B < 256u ? B : B / 256u;
+            rgba[pi] = R | (G << 8) | (B << 16);
+        } else {
+            rgba[pi] = 0u;
+        }
     }
 }
 
@@ -474,6 +478,35 @@ cr_status cuda_status(cudaError_t e) {
 }
 
 }  // namespace
+
+cr_status cr::encode_records_device(const uint8_t* d_rec, int64_t n, int32_t bpp, int32_t rgb,
+                                   const double scale[3], const double offset[3], const double box_min[3],
+                                   int64_t sparse_offset, int32_t file_index, cr_batch* d_batches,
+                                   uint32_t* d_lo, uint32_t* d_md, uint32_t* d_hi, uint32_t* d_rgba,
+                                   void* stream) {
+    if (n < 0 || (n > 0 && !d_rec) || bpp < 12 || !scale || !offset || !box_min || !d_batches || !d_lo ||
+        !d_md || !d_hi || !d_rgba || sparse_offset < 0 || sparse_offset + n >= ((int64_t)1 << 31))
+        return CR_ERR_INVALID_ARG;
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(scale[k]) || !std::isfinite(offset[k]) || !std::isfinite(box_min[k]))
+            return CR_ERR_INVALID_ARG;
+    if (rgb >= 0 && rgb + 6 > bpp) return CR_ERR_INVALID_ARG;
+    const int64_t nb = cr_num_batches(n);
+    if (nb == 0) return CR_OK;
+    EncodeArgs a;
+    for (int k = 0; k < 3; k++) {
+        a.scale[k] = scale[k];
+        a.offset[k] = offset[k];
+        a.box_min[k] = box_min[k];
+    }
+    a.n = n;
+    a.sparse_offset = sparse_offset;
+    a.bpp = bpp;
+    a.rgb = rgb < 0 ? -1 : rgb;
+    a.file_index = file_index;
+    k_encode<<<(unsigned)nb, 256, 0, (cudaStream_t)stream>>>(a, d_rec, d_batches, d_lo, d_md, d_hi, d_rgba);
+    return cuda_status(cudaGetLastError());
+}
 
 extern "C" {
 
@@ -604,30 +637,11 @@ cr_status cr_encode_las_device(cr_ctx* ctx, const uint8_t* d_rec, int64_t n, int
                                int64_t sparse_offset, int32_t file_index, cr_batch* d_batches,
                                uint32_t* d_lo, uint32_t* d_md, uint32_t* d_hi, uint32_t* d_rgba,
                                void* stream) {
-    if (!ctx || n < 0 || (n > 0 && !d_rec) || bpp < 12 || !scale || !offset || !box_min ||
-        !d_batches || !d_lo || !d_md || !d_hi || !d_rgba || sparse_offset < 0 ||
-        sparse_offset + n >= ((int64_t)1 << 31))
-        return CR_ERR_INVALID_ARG;
-    for (int k = 0; k < 3; k++)
-        if (!std::isfinite(scale[k]) || !std::isfinite(offset[k]) || !std::isfinite(box_min[k]))
-            return CR_ERR_INVALID_ARG;
+    if (!ctx) return CR_ERR_INVALID_ARG;
+    // LasLoaderSparse.cpp:123-131: formats without RGB read their colour at byte 0
     const int rgb = fmt == 2 ? 20 : (fmt == 3 ? 28 : ((fmt == 7 || fmt == 8) ? 30 : 0));
-    if (rgb != 0 && rgb + 6 > bpp) return CR_ERR_INVALID_ARG;
-    const int64_t nb = cr_num_batches(n);
-    if (nb == 0) return CR_OK;
-    EncodeArgs a;
-    for (int k = 0; k < 3; k++) {
-        a.scale[k] = scale[k];
-        a.offset[k] = offset[k];
-        a.box_min[k] = box_min[k];
-    }
-    a.n = n;
-    a.sparse_offset = sparse_offset;
-    a.bpp = bpp;
-    a.rgb = rgb;
-    a.file_index = file_index;
-    k_encode<<<(unsigned)nb, 256, 0, (cudaStream_t)stream>>>(a, d_rec, d_batches, d_lo, d_md, d_hi, d_rgba);
-    return cuda_status(cudaGetLastError());
+    return cr::encode_records_device(d_rec, n, bpp, rgb, scale, offset, box_min, sparse_offset, file_index,
+                                     d_batches, d_lo, d_md, d_hi, d_rgba, stream);
 }
 
 cr_status cr_synth_cloud_device(cr_ctx* ctx, const cr_synth_params* p, int64_t n, cr_cloud* cloud,

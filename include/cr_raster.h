@@ -49,7 +49,8 @@ typedef enum cr_status {
     CR_ERR_CUDA = 5,
     CR_ERR_DEVICE_FLAG = 6, /* a kernel found an out-of-range record and skipped it */
     CR_ERR_UNSUPPORTED = 7,
-    CR_ERR_NOT_FOUND = 8
+    CR_ERR_NOT_FOUND = 8,
+    CR_ERR_CORRUPT = 9 /* a compressed stream does not decode */
 } cr_status;
 
 /* Method ids; names as registered by the reference (compute_loop_las.h:82,

@@ -15,6 +15,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 GLMREF = HERE / "_ref" / "libglmref.so"
 SFREF = HERE / "_ref" / "libsfref.so"
+LAZREF = HERE / "_ref" / "liblaszipref.so"
 
 L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS, UVEC4_BASE, RESOLVE_TILES = 1, 2, 4, 8, 16
 NODE_LOOP, LEVEL4_80PX, ONE_WORLD = 32, 64, 128
@@ -122,6 +123,19 @@ def sfref() -> C.CDLL:
     g = C.CDLL(str(SFREF))
     g.sfref_morton.argtypes = [C.c_uint32] * 3
     g.sfref_morton.restype = C.c_uint64
+    return g
+
+
+def laszipref() -> C.CDLL:
+    """The LASzip probe built from the reference's vendored LASzip (oracle/_ref)."""
+    g = C.CDLL(str(LAZREF))
+    P, I, I64, U32 = C.c_void_p, C.c_int, C.c_int64, C.c_uint32
+    g.lzref_vlr.argtypes = [I, I, I, U32, P, C.c_int32]
+    g.lzref_vlr.restype = C.c_int
+    g.lzref_compress.argtypes = [P, I64, P, I64, I, I, I, U32, I64, P, I64]
+    g.lzref_compress.restype = I64
+    g.lzref_decompress.argtypes = [P, I64, I64, P, C.c_int32, I64, I, P]
+    g.lzref_decompress.restype = I64
     return g
 
 

@@ -210,3 +210,102 @@ def las2_visits(first, num_points, inclusive=True, threads=128, per_thread=80):
             if done:
                 break
     return sorted(out)
+
+
+LAZ_BASE_BYTES = {0: 20, 1: 28, 2: 26, 3: 34}
+
+
+def _mix(seed: int, i: np.ndarray, lane: int) -> np.ndarray:
+    """splitmix64 of (seed, index, lane): integer-only, the same on every host."""
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + i.astype(np.uint64) * np.uint64(0xBF58476D1CE4E5B9)
+             + np.uint64(lane) * np.uint64(0x94D049BB133111EB))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def laz_records(fmt: int, n: int, seed: int, extra: int = 0) -> tuple[np.ndarray, int]:
+    """LAS point format 0-3 records (plus `extra` bytes) whose every field
+    varies the way scans do: coordinates as random walks, intensity drifting,
+    runs of equal return bytes, classes and source IDs, scan angle steps, GPS
+    times rising with repeats and jumps (so LASzip's four time sequences and
+    full 64-bit codes are used), 8- and 16-bit and grey colours.  Integer-only
+    arithmetic: the same bytes on every host.  -> (records uint8, bpp)."""
+    bpp = LAZ_BASE_BYTES[fmt] + extra
+    i = np.arange(n, dtype=np.uint64)
+    h = [_mix(seed, i, lane) for lane in range(16)]
+    out = np.zeros((n, bpp), np.uint8)
+    step = lambda hh, r: (hh % np.uint64(2 * r + 1)).astype(np.int64) - r
+    xyz = np.stack([1_000_000 + np.cumsum(step(h[0], 1000)), 2_000_000 + np.cumsum(step(h[1], 1000)),
+                    50_000 + np.cumsum(step(h[2], 120))], axis=1).astype("<i4")
+    out[:, :12] = xyz.view(np.uint8).reshape(n, 12)
+    inten = (30000 + np.cumsum(step(h[3], 40))) % 65536
+    out[:, 12:14] = inten.astype("<u2").view(np.uint8).reshape(n, 2)
+    nret = 1 + (h[4] % np.uint64(5)).astype(np.int64)
+    ret = np.minimum(1 + (h[5] % np.uint64(5)).astype(np.int64), nret)
+    flags = (ret | (nret << 3) | ((h[6] & np.uint64(1)).astype(np.int64) << 6)
+             | ((h[6] % np.uint64(97) == 0).astype(np.int64) << 7)).astype(np.uint8)
+    keep = (h[7] % np.uint64(10)) < 7
+    flags[keep] = flags[0]
+    out[:, 14] = flags
+    out[:, 15] = (_mix(seed, i // np.uint64(100), 20) % np.uint64(20)).astype(np.uint8)
+    out[:, 16] = (np.cumsum(step(h[8], 1)) % 256).astype(np.uint8)
+    ud = (h[9] % np.uint64(256)).astype(np.uint8)
+    ud[(h[10] % np.uint64(20)) != 0] = 7
+    out[:, 17] = ud
+    out[:, 18:20] = (_mix(seed, i // np.uint64(5000), 21) % np.uint64(65536)).astype("<u2") \
+        .view(np.uint8).reshape(n, 2)
+    off = 20
+    if fmt in (1, 3):
+        ticks = (100_000 << 20) + np.cumsum((h[11] % np.uint64(64)).astype(np.int64))
+        jump = (h[12] % np.uint64(997)) == 0
+        ticks[jump] += ((h[13][jump] % np.uint64(2 << 34)).astype(np.int64) - (1 << 34))
+        same = (h[12] % np.uint64(20)) == 1
+        ticks[same] = ticks[0]
+        t = ticks.astype(np.float64) / float(1 << 20)
+        out[:, off:off + 8] = t.astype("<f8").view(np.uint8).reshape(n, 8)
+        off += 8
+    if fmt in (2, 3):
+        rgb = np.stack([(h[14] >> np.uint64(8 * k)) % np.uint64(256) for k in range(3)], axis=1)
+        wide = (h[15] % np.uint64(8)) != 0
+        rgb[wide] *= np.uint64(256)
+        grey = (h[15] % np.uint64(5)) == 0
+        rgb[grey, 1] = rgb[grey, 0]
+        rgb[grey, 2] = rgb[grey, 0]
+        out[:, off:off + 6] = rgb.astype("<u2").view(np.uint8).reshape(n, 6)
+        off += 6
+    if extra:
+        out[:, off:] = ((i[:, None] // np.uint64(7) + np.arange(extra, dtype=np.uint64)[None, :] * np.uint64(3))
+                        % np.uint64(256)).astype(np.uint8)
+    return out.reshape(-1), bpp
+
+
+LAZ_SCALE, LAZ_OFFSET = (0.001, 0.001, 0.001), (0.0, 0.0, 0.0)
+
+
+def laz_box(records: np.ndarray, n: int, bpp: int):
+    xyz = records.reshape(n, bpp)[:, :12].copy().view("<i4").reshape(n, 3).astype(np.float64) * 0.001
+    return tuple(xyz.min(0)), tuple(xyz.max(0))
+
+
+def laszip_file(records: np.ndarray, n: int, fmt: int, bpp: int, chunk: int = 50000, var_every: int = 0,
+                compressor: int = 2) -> bytes:
+    """A LAZ file whose point data LASzip itself wrote (the reference's vendored
+    codec built into oracle/_ref), under the same LAS header and VLR framing
+    as compute_rasterizer_gb300.las.laz_bytes."""
+    from compute_rasterizer_gb300 import las
+    lz = O.laszipref()
+    vlr = np.zeros(256, np.uint8)
+    vn = lz.lzref_vlr(fmt, bpp, compressor, chunk & 0xFFFFFFFF, vlr.ctypes.data, 256)
+    assert vn > 0
+    bmin, bmax = laz_box(records, n, bpp)
+    head = las._header(n, LAZ_SCALE, LAZ_OFFSET, bmin, bmax, fmt | 128, bpp, (1, 2),
+                       [("laszip encoder", 22204, vlr[:vn].tobytes())])
+    pre = np.frombuffer(head, np.uint8).copy()
+    rec = np.ascontiguousarray(records, np.uint8)
+    out = np.zeros(n * bpp * 2 + 65536, np.uint8)
+    size = lz.lzref_compress(pre.ctypes.data, pre.size, rec.ctypes.data, n, fmt, bpp, compressor,
+                             chunk & 0xFFFFFFFF, var_every, out.ctypes.data, out.size)
+    assert size > 0, size
+    return out[:size].tobytes()

@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--cpu-table", action="store_true",
                     help="time the oracle per workload on this host's cores and exit")
     ap.add_argument("--serving", default="quick", choices=["quick", "full", "off"])
-    ap.add_argument("--extras", default="payloads,multiview,configs,serving",
+    ap.add_argument("--extras", default="payloads,multiview,configs,serving,ingest",
                     help="comma list of extra workloads after the headline frame")
     return ap.parse_args()
 
@@ -408,7 +408,8 @@ def main():
         want = set(args.extras.split(","))
         runs = [("payloads", lambda: extras(ctx, cloud, cv, fb, sh, n, args)),
                 ("multiview", lambda: {"multiview_64": multiview_64(ctx, sh, args.steps, payload)}),
-                ("configs", lambda: small_configs(ctx, sh, args, payload))]
+                ("configs", lambda: small_configs(ctx, sh, args, payload)),
+                ("ingest", lambda: {"ingest": ingest(ctx, sh)})]
         if args.serving != "off":
             runs.append(("serving", lambda: {"serving": serving(ctx, sh, args, payload)}))
         for name, fn in runs:
@@ -473,6 +474,84 @@ def extras(ctx, cloud, cv, fb, sh, n, args):
     return res
 
 
+def ingest(ctx, sh, points=50_000_000):
+    """File ingest (LasLoaderSparse.cpp:477-713 with loadLas / loadLaz): a
+    Morton-sorted terrain of `points` format-2 records (generated and sorted on
+    the GPU, read back) written as LAS bytes in host memory and as LAZ by the
+    product's writer; each loaded into a cloud through the C ABI (host
+    records -> load tasks -> GPU encoder; LAZ: parallel chunk decode on all host
+    threads overlapping upload and encode).  Wall-clock, one run each after a
+    warm-up on a small file; the two clouds are compared word for word."""
+    import ctypes as C
+    import os
+    import time
+
+    import torch
+
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import las, synth
+    lib = L.load()
+    n, bpp = points, L.LAS_FORMAT2_BYTES
+    p = synth.synth_params(L.SYNTH_TERRAIN, 3000.0, 77)
+    hdr = L.LasHeader()
+    rec_d = torch.empty(n * bpp, dtype=torch.uint8, device="cuda")
+    ctx.check(lib.cr_synth_points_device(ctx.handle, C.byref(p), n, rec_d.data_ptr(), C.byref(hdr), sh), "gen")
+    ctx.check(lib.cr_morton_sort_device(ctx.handle, rec_d.data_ptr(), n, bpp, C.byref(hdr), sh), "sort")
+    ctx.sync(sh)
+    rec = rec_d.cpu().numpy()
+    del rec_d
+    torch.cuda.empty_cache()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    laz = las.laz_bytes(rec, n, hdr.scale, hdr.offset, hdr.min, hdr.max, threads=0)
+    write_s = time.perf_counter() - t0
+    info = las.parse_header(las._header(n, hdr.scale, hdr.offset, hdr.min, hdr.max, 2, bpp, (1, 2)))
+    nb = int(lib.cr_las_num_batches(n))
+    lz = las.LazFile(laz)
+
+    def load_las():
+        c = ctx.cloud(n, nb, 1)
+        t = time.perf_counter()
+        ctx.check(lib.cr_cloud_load_las(ctx.handle, c.handle, rec.ctypes.data, n, C.byref(info), 0, 0, 0, sh),
+                  "load las")
+        return c, time.perf_counter() - t
+
+    def load_laz():
+        c = ctx.cloud(n, nb, 1)
+        t = time.perf_counter()
+        ctx.check(lib.cr_cloud_load_laz(ctx.handle, c.handle, lz.handle, 0, 0, 0, 0, sh), "load laz")
+        return c, time.perf_counter() - t
+
+    small = las.LazFile(las.laz_bytes(rec[:2_000_000 * bpp], 2_000_000, hdr.scale, hdr.offset, hdr.min,
+                                      hdr.max))
+    warm = ctx.cloud(2_000_000, int(lib.cr_las_num_batches(2_000_000)), 1)
+    ctx.check(lib.cr_cloud_load_laz(ctx.handle, warm.handle, small.handle, 0, 0, 0, 0, sh), "warm-up")
+    warm.close()
+    c_las, las_s = load_las()
+    c_laz, laz_s = load_laz()
+    same = all(np.array_equal(c_las.read(w), c_laz.read(w)) for w in
+               (0, L.STREAM_LOW, L.STREAM_MED, L.STREAM_HIG, L.STREAM_RGBA))
+    c_las.close()
+    c_laz.close()
+    sub = 5_000_000
+    t = time.perf_counter()
+    lz.decode(0, sub, threads=1)
+    one_s = time.perf_counter() - t
+    t = time.perf_counter()
+    lz.decode(threads=0)
+    dec_s = time.perf_counter() - t
+    return {"points": n, "host_threads": threads, "laz_bytes": len(laz),
+            "laz_bytes_per_point": round(len(laz) / n, 3),
+            "las_load_mpts_per_s": round(n / las_s / 1e6, 1),
+            "laz_load_mpts_per_s": round(n / laz_s / 1e6, 1),
+            "laz_decode_mpts_per_s": round(n / dec_s / 1e6, 1),
+            "laz_decode_1thread_mpts_per_s": round(sub / one_s / 1e6, 2),
+            "laz_write_mpts_per_s": round(n / write_s / 1e6, 1),
+            "laz_equals_las_cloud": bool(same),
+            "what": "cr_cloud_load_las / cr_cloud_load_laz wall clock from host memory; decode-only "
+                    "cr_laz_decode on all threads and on one (5M points)"}
+
+
 def multiview_64(ctx, sh, steps, payload):
     """200M points (terrain + 2000 boxes), 64 views: the multi-view plan
     (autotuned, CUDA graph) against one cr_render per view, images compared."""
@@ -518,10 +597,28 @@ def multiview_64(ctx, sh, steps, payload):
     plain_ms = ev[2].elapsed_time(ev[3]) / k
     same = all(np.array_equal(mv.read(i, L.FB_IMAGE, sh), f.read(L.FB_IMAGE, sh))
                for i, f in enumerate(fbs))
+    pairs = mv.shared_pairs()
+    # A/B of the stereo sharing: the eyes built by look_at from their own
+    # positions (same cameras up to rounding, rows not bitwise equal)
+    mv.set_views([cr.make_view(*c) for c in workloads.multiview_64(np.array(hdr.min[:]), np.array(hdr.max[:]),
+                                                                    compose_eyes=False)])
+    unshared_pairs = mv.shared_pairs()
+    for _ in range(3):
+        mv.render(True, sh)
+    ctx.sync(sh)
+    ev[0].record(stream)
+    for _ in range(k):
+        mv.render(True, sh)
+    ev[1].record(stream)
+    ctx.sync(sh)
+    unshared_ms = ev[0].elapsed_time(ev[1]) / k
     out = {"points": n, "views": len(cams), "payload": "color" if payload else "index",
            "batched_ms_per_frame": round(mv_ms, 3), "plain_ms_per_frame": round(plain_ms, 3),
            "batched_frames_per_s": round(1e3 / mv_ms, 2), "plain_frames_per_s": round(1e3 / plain_ms, 2),
            "speedup_vs_plain": round(plain_ms / mv_ms, 3), "bit_exact_images": bool(same),
+           "shared_stereo_pairs": pairs,
+           "eyes_by_look_at": {"shared_stereo_pairs": unshared_pairs,
+                               "batched_ms_per_frame": round(unshared_ms, 3)},
            "autotuned": {"block_threads": best.block_threads, "views_per_group": best.views_per_group,
                          "points_per_thread": 10240 // max(1, best.block_threads)},
            "autotune_ms": report,

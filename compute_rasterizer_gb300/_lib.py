@@ -206,6 +206,7 @@ _SIGS = {
     "cr_mv_last_error": (C.c_char_p, [P]),
     "cr_mv_set_params": (I32, [P, C.POINTER(RenderParams)]),
     "cr_mv_get_params": (I32, [P, C.POINTER(RenderParams)]),
+    "cr_mv_shared_pairs": (I32, [P, C.POINTER(I32)]),
     "cr_mv_set_views": (I32, [P, C.POINTER(View)]),
     "cr_mv_render": (I32, [P, I32, P]),
     "cr_mv_clear": (I32, [P, U64, P]),

@@ -214,6 +214,8 @@ struct MVFrame {
     // memory; the frame computes d_files from them before the cull
     const double* d_mats;
     const double* d_box;
+    // per view group, bit s: views s and s + 1 share their y / w rows (or NULL)
+    const uint32_t* d_pairs;
 };
 int64_t mv_scratch_words(int64_t nb, int64_t nviews);
 // Enqueues counter reset, [fill], cull, raster (both lists), [resolve] on stream.

@@ -42,6 +42,7 @@ struct MVArgs {
     uint32_t* scratch;
     int64_t list_cap;  // uint4 items in the list region: batches x groups
     int32_t quirks;
+    const uint32_t* pairs;  // per group: bit s = views s, s + 1 share rows y and w (or NULL)
 };
 
 constexpr int kSlotWords = 16;  // per view slot in shared memory: T[12], Wf, Hf, W, fb_off
@@ -227,6 +228,53 @@ __device__ __forceinline__ void splat_view(const MVArgs& a, unsigned long long* 
     }
 }
 
+// Two views whose T rows y and w are bitwise equal (a stereo pair built as
+// translate(-+ipd/2, 0, 0) * V_head, whose eyes differ in row x only) and whose
+// slots hold the same Wf, Hf and W: y, w, 1/w, the inside test of y and the
+// pixel row are computed once per point, x and the pixel column per view.
+// Every value is the one splat_view computes (same operations, same operands),
+// so both views' words are unchanged.
+template <int PAYLOAD, bool SAFE>
+__device__ __forceinline__ void splat_pair(const MVArgs& a, unsigned long long* zc, const float* sa,
+                                           const float* sb, const Decoded& d, uint32_t valid_mask,
+                                           uint32_t idx0, const uint4& col) {
+    const float4 t0 = reinterpret_cast<const float4*>(sa)[0];
+    const float4 t1 = reinterpret_cast<const float4*>(sa)[1];
+    const float4 t2 = reinterpret_cast<const float4*>(sa)[2];
+    const float4 t3 = reinterpret_cast<const float4*>(sa)[3];
+    const float4 u0 = reinterpret_cast<const float4*>(sb)[0];
+    const float4 u1 = reinterpret_cast<const float4*>(sb)[1];
+    const float4 u2 = reinterpret_cast<const float4*>(sb)[2];
+    const float4 u3 = reinterpret_cast<const float4*>(sb)[3];
+    // slot layout T0 T1 T3 T4 | T5 T7 T8 T9 | T11 T12 T13 T15 | Wf Hf W fb_off
+    const float aT0 = t0.x, aT1 = t0.y, aT3 = t0.z, aT4 = t0.w, aT5 = t1.x, aT7 = t1.y, aT8 = t1.z;
+    const float aT9 = t1.w, aT11 = t2.x, aT12 = t2.y, aT13 = t2.z, aT15 = t2.w;
+    const float bT0 = u0.x, bT4 = u0.w, bT8 = u1.z, bT12 = u2.y;
+    const float Wf = t3.x, Hf = t3.y;
+    const int32_t W = __float_as_int(t3.z);
+    const uint32_t fa = __float_as_uint(t3.w), fb = __float_as_uint(u3.w);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float x = d.x[j], y = d.y[j], z = d.z[j];
+        const float py = __fmaf_rn(aT9, z, __fmaf_rn(aT5, y, __fmaf_rn(aT1, x, aT13)));
+        const float pw = __fmaf_rn(aT11, z, __fmaf_rn(aT7, y, __fmaf_rn(aT3, x, aT15)));
+        const float rw = SAFE ? rcp_rn_normal(pw) : rcp_rn(pw);
+        const float qy = fmul(py, rw);
+        const bool yin = ((valid_mask >> j) & 1u) && pw > 0.0f && qy >= -1.0f && qy <= 1.0f;
+        const int32_t row = small_f2i(fmul(__fmaf_rn(qy, 0.5f, 0.5f), Hf)) * W;
+        const uint32_t wbits = __float_as_uint(pw);
+        const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? u4get(col, j) : idx0 + (uint32_t)j;
+        const float pxa = __fmaf_rn(aT8, z, __fmaf_rn(aT4, y, __fmaf_rn(aT0, x, aT12)));
+        const float qxa = fmul(pxa, rw);
+        const bool oka = yin && qxa >= -1.0f && qxa <= 1.0f;
+        emit_mv(a.fbs, zc, oka, small_f2i(fmul(__fmaf_rn(qxa, 0.5f, 0.5f), Wf)) + row, fa, wbits, payload);
+        const float pxb = __fmaf_rn(bT8, z, __fmaf_rn(bT4, y, __fmaf_rn(bT0, x, bT12)));
+        const float qxb = fmul(pxb, rw);
+        const bool okb = yin && qxb >= -1.0f && qxb <= 1.0f;
+        emit_mv(a.fbs, zc, okb, small_f2i(fmul(__fmaf_rn(qxb, 0.5f, 0.5f), Wf)) + row, fb, wbits, payload);
+    }
+}
+
 // LIST 0: items whose visible views all decode at 10 bit (only the low word
 // stream is read); LIST 1: the others, each view decoded at its own level.
 template <int PAYLOAD, int BLOCK, int LIST>
@@ -277,6 +325,19 @@ __device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
                 if ((vismask >> s) & 1u) classes |= 1u << level_class((levels >> (3 * s)) & 7u);
         const bool single = LIST == 0 || __popc(classes) == 1;
         const int only = LIST == 0 ? 2 : __ffs(classes) - 1;
+        // shared pairs of this item: both views visible, at one level class,
+        // with the same w-range proof
+        uint32_t pairs = 0;
+        if (a.pairs) {
+            const uint32_t cand = a.pairs[g] & vismask & (vismask >> 1);
+            for (int s = 0; s + 1 < a.G; s++) {
+                if (((cand >> s) & 1u) == 0u) continue;
+                const bool same_level =
+                    LIST == 0 || level_class((levels >> (3 * s)) & 7u) == level_class((levels >> (3 * s + 3)) & 7u);
+                const bool same_safe = (((levels >> (24 + s)) ^ (levels >> (25 + s))) & 1u) == 0u;
+                if (same_level && same_safe) pairs |= 1u << s;
+            }
+        }
         const bool need8 = LIST == 1 && (classes & 3u) != 0;
         const bool need12 = LIST == 1 && (classes & 1u) != 0;
         float sc[6];
@@ -333,10 +394,18 @@ __device__ __forceinline__ void mv_raster_items(const MVArgs& a) {
                             l0_x12, d);
                 // views whose w range is proven safe skip the reciprocal's range
                 // test (measured 12 % faster on the 64-view frame)
-                if ((levels >> (24 + s)) & 1u)
+                const bool safe = (levels >> (24 + s)) & 1u;
+                if ((pairs >> s) & 1u) {
+                    if (safe)
+                        splat_pair<PAYLOAD, true>(a, s_zc, s_view[s], s_view[s + 1], d, valid_mask, idx0, col);
+                    else
+                        splat_pair<PAYLOAD, false>(a, s_zc, s_view[s], s_view[s + 1], d, valid_mask, idx0, col);
+                    s++;
+                } else if (safe) {
                     splat_view<PAYLOAD, true>(a, s_zc, s_view[s], d, valid_mask, idx0, col);
-                else
+                } else {
                     splat_view<PAYLOAD, false>(a, s_zc, s_view[s], d, valid_mask, idx0, col);
+                }
             }
         }
         __syncthreads();
@@ -522,6 +591,7 @@ cr_status mv_enqueue(const MVFrame& f, void* stream, const char** what) {
         a.scratch = f.scratch;
         a.list_cap = threads;  // k_mv_cull's list region: one item per (batch, group)
         a.quirks = f.quirks;
+        a.pairs = f.d_pairs;
         const bool color = f.payload == CR_PAYLOAD_COLOR;
         const int per_sm = f.ctas_per_sm > 0 ? f.ctas_per_sm
                            : (color ? mv_occupancy_t<CR_PAYLOAD_COLOR>(f.block)
@@ -564,6 +634,10 @@ struct cr_mv {
     double* d_mats = nullptr;   // and every file's boxMin, from which each frame
     double* h_box = nullptr;    // computes d_files on the GPU
     double* d_box = nullptr;
+    std::vector<uint8_t> eq_next;  // view v shares rows y and w with view v + 1
+    uint32_t* h_pairs = nullptr;   // per group: bit s pairs views s, s + 1 (pinned)
+    uint32_t* d_pairs = nullptr;
+    int32_t shared_pairs = 0;
     uint32_t* scratch = nullptr;
     int num_sms = 0;
     cr_render_params params{};
@@ -596,6 +670,41 @@ void drop_graph(cr_mv* mv) {
     mv->graph = nullptr;
 }
 
+// Greedy disjoint pairs (s, s + 1) inside each group of G views.
+void update_pairs(cr_mv* mv) {
+    if (!mv->h_pairs) return;
+    mv->shared_pairs = 0;
+    for (int g = 0; g < mv->ngroups; g++) {
+        uint32_t mask = 0;
+        for (int s = 0; s + 1 < mv->G; s++) {
+            const int v = g * mv->G + s;
+            if (v + 1 >= mv->nviews) break;
+            if (mv->eq_next.size() > (size_t)v && mv->eq_next[v]) {
+                mask |= 1u << s;
+                ++mv->shared_pairs;
+                ++s;
+            }
+        }
+        mv->h_pairs[g] = mask;
+    }
+}
+
+// Views v and v + 1 share their projected y, w: equal size and proj * view
+// rows 1 and 3 bitwise equal.  Every file's transform row r is computed from
+// row r of proj * view and the file's boxMin alone (file_record:
+// (proj * view) * translate(boxMin)), so the float rows y and w of all the
+// files' T then agree too.
+bool shares_rows(const cr_view& a, const cr_view& b) {
+    if (a.width != b.width || a.height != b.height) return false;
+    double pa[16], pb[16];
+    mat_mul(a.proj, a.view, pa);
+    mat_mul(b.proj, b.view, pb);
+    for (int c = 0; c < 4; c++)
+        for (int row : {1, 3})
+            if (std::memcmp(&pa[4 * c + row], &pb[4 * c + row], sizeof(double)) != 0) return false;
+    return true;
+}
+
 cr_status apply_params(cr_mv* mv, const cr_render_params* p) {
     if (p->method != CR_METHOD_LOOP_LAS && p->method != CR_METHOD_LOOP_LAS_PREFETCH)
         return mv_fail(mv, CR_ERR_INVALID_ARG, "multi-view plans render loop_las / loop_las_prefetch");
@@ -614,6 +723,7 @@ cr_status apply_params(cr_mv* mv, const cr_render_params* p) {
     mv->ngroups = (mv->nviews + mv->G - 1) / mv->G;
     mv->block = block;
     mv->quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? default_quirks_for(p->method) : p->quirks;
+    update_pairs(mv);
     return CR_OK;
 }
 
@@ -631,6 +741,9 @@ cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
                             cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && many)
         e = cudaMemcpyAsync(mv->d_box, mv->h_box, sizeof(double) * 3 * (size_t)mv->ci.nfiles,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(mv->d_pairs, mv->h_pairs, sizeof(uint32_t) * (size_t)mv->ngroups,
                             cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return mv_cuda(mv, e, "frame setup");
     MVFrame f{};
@@ -656,6 +769,7 @@ cr_status enqueue_frame(cr_mv* mv, cudaStream_t st) {
     f.max_words = mv->max_words;
     f.d_mats = mv->d_mats;
     f.d_box = mv->d_box;
+    f.d_pairs = mv->d_pairs;
     const char* what = "";
     const cr_status s = mv_enqueue(f, st, &what);
     if (s != CR_OK) return mv_fail(mv, s, std::string(what) + " failed");
@@ -703,6 +817,7 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
     }
     mv->total_words = words;
     mv->total_pixels = pixels;
+    mv->eq_next.assign(nviews, 0);
     cr_status s = apply_params(mv, params);
     if (s != CR_OK) {
         delete mv;
@@ -715,6 +830,12 @@ cr_status cr_mv_create(cr_ctx* ctx, const cr_cloud* cloud, int32_t nviews, const
     if (e == cudaSuccess) e = cudaMalloc(&mv->scratch, mv_scratch_words(mv->ci.nb_total, nviews) * 4);
     if (e == cudaSuccess) e = cudaMemset(mv->scratch, 0, mv_scratch_words(mv->ci.nb_total, nviews) * 4);
     if (e == cudaSuccess) e = cudaHostAlloc(&mv->h_views, sizeof(MVView) * nviews, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc(&mv->d_pairs, sizeof(uint32_t) * nviews);
+    if (e == cudaSuccess) e = cudaHostAlloc(&mv->h_pairs, sizeof(uint32_t) * nviews, cudaHostAllocDefault);
+    if (e == cudaSuccess) {
+        std::memset(mv->h_pairs, 0, sizeof(uint32_t) * nviews);
+        update_pairs(mv);
+    }
     if (mv->ci.nfiles <= kInlineFiles) {
         if (e == cudaSuccess)
             e = cudaHostAlloc(&mv->h_files, sizeof(MVFile) * (size_t)nviews * mv->ci.nfiles,
@@ -746,10 +867,11 @@ cr_status cr_mv_destroy(cr_mv* mv) {
     if (!mv) return CR_ERR_INVALID_ARG;
     if (mv->pending) cudaEventSynchronize(mv->done);
     drop_graph(mv);
-    void* dev[7] = {mv->fbs, mv->images, mv->d_views, mv->d_files, mv->scratch, mv->d_mats, mv->d_box};
+    void* dev[8] = {mv->fbs, mv->images, mv->d_views, mv->d_files, mv->scratch, mv->d_mats, mv->d_box,
+                    mv->d_pairs};
     for (void* p : dev)
         if (p) cudaFree(p);
-    void* host[4] = {mv->h_views, mv->h_files, mv->h_mats, mv->h_box};
+    void* host[5] = {mv->h_views, mv->h_files, mv->h_mats, mv->h_box, mv->h_pairs};
     for (void* p : host)
         if (p) cudaFreeHost(p);
     if (mv->done) cudaEventDestroy(mv->done);
@@ -794,7 +916,16 @@ cr_status cr_mv_set_views(cr_mv* mv, const cr_view* views) {
     }
     // the files' boxMin as the frames of these views read them
     if (mv->h_box) std::memcpy(mv->h_box, mv->ci.box_min, sizeof(double) * 3 * (size_t)mv->ci.nfiles);
+    for (int v = 0; v < mv->nviews; v++)
+        mv->eq_next[v] = v + 1 < mv->nviews && shares_rows(views[v], views[v + 1]) ? 1 : 0;
+    update_pairs(mv);
     mv->views_set = true;
+    return CR_OK;
+}
+
+cr_status cr_mv_shared_pairs(const cr_mv* mv, int32_t* pairs) {
+    if (!mv || !pairs) return CR_ERR_INVALID_ARG;
+    *pairs = mv->shared_pairs;
     return CR_OK;
 }
 

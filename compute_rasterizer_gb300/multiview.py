@@ -42,6 +42,12 @@ class MultiView:
         arr = (L.View * len(views))(*views)
         self._check(self.lib.cr_mv_set_views(self.handle, arr), "set views")
 
+    def shared_pairs(self) -> int:
+        """View pairs whose y / w projection rows the frame computes once."""
+        n = C.c_int32()
+        self._check(self.lib.cr_mv_shared_pairs(self.handle, C.byref(n)), "shared pairs")
+        return n.value
+
     def render(self, use_graph: bool = False, stream=None):
         self._check(self.lib.cr_mv_render(self.handle, int(use_graph), stream), "render")
 

@@ -5,8 +5,9 @@ Seeded, so every run renders the same frames:
                        (src/main.cpp:251-270), 1920x1080.
   * flight_path        5 poses along a seeded flight over a terrain, 2560x1440.
   * multiview_64       16 stereo pairs at 1440x1600 per eye (IPD 0.064 m,
-                       parallel eye axes) flying over the cloud + 32 random
-                       orbit poses at 512x512.
+                       parallel eye axes: each eye translate(-+ipd/2, 0, 0) *
+                       V_head, as a headset composes them) flying over the
+                       cloud + 32 random orbit poses at 512x512.
   * serving            8 resident terrains of 10-500 M points, Poisson
                        arrivals, clouds drawn Zipf(1.1), one random orbit
                        camera per request at one of five resolutions.
@@ -53,8 +54,19 @@ def _look_dir(yaw, pitch):
     return np.array([math.cos(pitch) * math.cos(yaw), math.cos(pitch) * math.sin(yaw), math.sin(pitch)])
 
 
-def multiview_64(box_min, box_max, seed=4, ipd=0.064):
-    """16 stereo pairs (1440x1600 per eye) + 32 random poses (512x512)."""
+def eye_view(head_view, dx: float) -> np.ndarray:
+    """translate(dx, 0, 0) * head_view (column-major doubles): an eye's view
+    from the head's; only the x translation (element 12) changes."""
+    v = np.array(head_view, dtype=np.float64).reshape(16).copy()
+    v[12] = v[12] + dx
+    return v
+
+
+def multiview_64(box_min, box_max, seed=4, ipd=0.064, compose_eyes=True):
+    """16 stereo pairs (1440x1600 per eye) + 32 random poses (512x512).
+    compose_eyes=False builds each eye by look_at from its own position
+    instead: the same cameras up to rounding, but the eyes' projection rows
+    no longer agree bit for bit, so a multi-view plan cannot share them."""
     rng = np.random.default_rng(seed)
     bmin, bmax = np.asarray(box_min, float), np.asarray(box_max, float)
     size = bmax - bmin
@@ -64,11 +76,16 @@ def multiview_64(box_min, box_max, seed=4, ipd=0.064):
         centre = bmin + size * np.array([rng.uniform(0.15, 0.85), rng.uniform(0.15, 0.85), 1.0])
         centre[2] = bmax[2] + rng.uniform(20.0, 150.0)
         d = _look_dir(rng.uniform(-math.pi, math.pi), rng.uniform(-0.6, -0.15))
+        head = synth.look_at(centre, centre + d, up)
         right = np.cross(d, up)
         right /= np.linalg.norm(right)
-        for side in (-0.5, 0.5):
-            eye = centre + side * ipd * right
-            cams.append((synth.look_at(eye, eye + d, up), _perspective(90.0, 1440, 1600), 1440, 1600))
+        for side in (-0.5, 0.5):  # the eye at centre + side * ipd * right
+            if compose_eyes:
+                view = eye_view(head, -side * ipd)
+            else:
+                eye = centre + side * ipd * right
+                view = synth.look_at(eye, eye + d, up)
+            cams.append((view, _perspective(90.0, 1440, 1600), 1440, 1600))
     yaw0, pitch0, radius0, target0 = synth.zoom_to_cloud(bmin, bmax)
     for _ in range(32):
         target = bmin + size * np.array([rng.uniform(0.1, 0.9), rng.uniform(0.1, 0.9), 0.5])

@@ -292,8 +292,15 @@ const char* cr_mv_last_error(const cr_mv* mv);
 cr_status cr_mv_set_params(cr_mv* mv, const cr_render_params* params);
 cr_status cr_mv_get_params(const cr_mv* mv, cr_render_params* out);
 /* Sets all num_views cameras (sizes must match the plan).  Waits for the
- * previous frame's uniform upload before overwriting the staging copy. */
+ * previous frame's uniform upload before overwriting the staging copy.
+ * Adjacent views of a group whose proj * view rows y and w are bitwise equal
+ * (the eyes of a stereo pair built as translate(-+ipd/2, 0, 0) * V_head, of
+ * equal size) become a shared pair: each point's y, w, 1/w and pixel row are
+ * computed once for both, x and the pixel column per eye -- the same
+ * operations on the same operands, so the words do not change. */
 cr_status cr_mv_set_views(cr_mv* mv, const cr_view* views);
+/* Number of view pairs the current views and views_per_group share. */
+cr_status cr_mv_shared_pairs(const cr_mv* mv, int32_t* pairs);
 /* Enqueues one frame on `stream`.  use_graph = 1 captures the frame into a
  * CUDA graph on the first call and replays it afterwards (needs a stream
  * other than the legacy default stream). */

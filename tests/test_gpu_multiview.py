@@ -146,3 +146,108 @@ def test_multiview_lod_cut_equals_single_views(ctx, scene):
         assert np.array_equal(got, want), (i, first_diff(got, want))
         fb.close()
     mv.close()
+
+
+def stereo_cams(cl, rng_seed=9):
+    """Stereo pairs (translate(-+ipd/2) * V_head, equal sizes) of the far,
+    near, mid and corner poses and of random orbits, with two decoys: a pair
+    of unequal sizes and a pair with different fields of view."""
+    from compute_rasterizer_gb300.workloads import eye_view
+    heads = list(camera_views(cl["box_min"], cl["box_max"], cl["batches"]).values())
+    rng = np.random.default_rng(rng_seed)
+    target = (cl["box_min"] + cl["box_max"]) / 2
+    for _ in range(3):
+        heads.append(synth.orbit_view(rng.uniform(-3, 3), rng.uniform(-1.3, -0.2), rng.uniform(5, 300),
+                                      target + rng.uniform(-60, 60, 3)))
+    cams, paired = [], []
+    for k, h in enumerate(heads):
+        w, hh = [(320, 240), (160, 176), (200, 150), (96, 96), (240, 240), (128, 160), (300, 200)][k]
+        proj = synth.perspective(90.0, w / hh, 0.1, 200000.0)
+        for side in (-0.5, 0.5):
+            cams.append((eye_view(h, -side * 0.064), proj, w, hh))
+        paired += [True, False]
+    # decoys: unequal sizes; unequal fields of view
+    h = heads[0]
+    cams.append((eye_view(h, 0.032), synth.perspective(90.0, 4 / 3, 0.1, 200000.0), 320, 240))
+    cams.append((eye_view(h, -0.032), synth.perspective(90.0, 4 / 3, 0.1, 200000.0), 160, 120))
+    cams.append((eye_view(h, 0.032), synth.perspective(90.0, 4 / 3, 0.1, 200000.0), 200, 150))
+    cams.append((eye_view(h, -0.032), synth.perspective(70.0, 4 / 3, 0.1, 200000.0), 200, 150))
+    paired += [False] * 4
+    return cams, paired
+
+
+def expected_pairs(paired, G):
+    count = 0
+    for g0 in range(0, len(paired), G):
+        s = 0
+        while s + 1 < G and g0 + s + 1 < len(paired):
+            if paired[g0 + s]:
+                count += 1
+                s += 2
+            else:
+                s += 1
+    return count
+
+
+@pytest.mark.parametrize("group,block", [(8, 128), (2, 64), (3, 128), (5, 256)])
+@pytest.mark.parametrize("payload", [L.PAYLOAD_INDEX, L.PAYLOAD_COLOR])
+def test_stereo_pairs_share_rows_bit_exact(ctx, scene, group, block, payload):
+    """Stereo eyes share y, w and 1/w: the plan finds the pairs (not the
+    decoys, not across group borders) and every view still equals cr_render
+    of that view alone, words and images, through graph replay too."""
+    import torch
+    cl, cloud, _ = scene
+    cams, paired = stereo_cams(cl)
+    params = default_params(L.METHOD_LOOP_LAS, payload=payload, views_per_group=group, block_threads=block)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    assert mv.shared_pairs() == expected_pairs(paired, group) > 0
+    s = torch.cuda.Stream()
+    mv.clear(stream=s.cuda_stream)
+    for _ in range(2):
+        mv.render(use_graph=True, stream=s.cuda_stream)
+    ctx.sync(s.cuda_stream)
+    p0 = default_params(L.METHOD_LOOP_LAS, payload=payload, views_per_group=group, block_threads=block,
+                        resolve=0, clear_after=0)
+    mv2 = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], p0)
+    mv2.set_views([make_view(*c) for c in cams])
+    mv2.clear()
+    mv2.render()
+    ctx.sync()
+    for i, cam in enumerate(cams):
+        want_w, want_img = single_view(ctx, cloud, cam, L.METHOD_LOOP_LAS, payload)
+        got = mv2.read(i, L.FB_WORDS)
+        assert np.array_equal(got, want_w), (i, first_diff(got, want_w))
+        assert np.array_equal(mv.read(i, L.FB_IMAGE, s.cuda_stream), want_img), i
+    mv.close()
+    mv2.close()
+
+
+def test_stereo_pairs_many_files_and_oracle(ctx):
+    """A 300-file cloud (file records computed on the GPU): shared pairs stay
+    bit-exact, against single views and against the oracle."""
+    from compute_rasterizer_gb300.workloads import eye_view
+    from helpers import many_file_cameras, many_file_cloud
+    cl = many_file_cloud()
+    cloud = ctx.cloud_from_arrays(cl["batches"], cl["lo"], cl["md"], cl["hi"], cl["rgba"], cl["box_min"])
+    cams = []
+    for cam in list(many_file_cameras(cl).values())[:3]:
+        for side in (-0.5, 0.5):
+            cams.append((eye_view(cam[0], -side * 0.064), cam[1], cam[2], cam[3]))
+    params = default_params(L.METHOD_LOOP_LAS, views_per_group=8, resolve=0, clear_after=0)
+    mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in cams], params)
+    mv.set_views([make_view(*c) for c in cams])
+    assert mv.shared_pairs() == 3
+    mv.clear()
+    mv.render()
+    ctx.sync()
+    for i, cam in enumerate(cams):
+        want, _ = single_view(ctx, cloud, cam, L.METHOD_LOOP_LAS, L.PAYLOAD_INDEX)
+        got = mv.read(i, L.FB_WORDS)
+        assert np.array_equal(got, want), (i, first_diff(got, want))
+        if i in (0, 3):
+            fr = oracle_frame(cam, cl["box_min"], QUIRKS[L.METHOD_LOOP_LAS])
+            ref = O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+            assert np.array_equal(got, ref), (i, first_diff(got, ref))
+    mv.close()
+    cloud.close()

@@ -612,6 +612,32 @@ def multiview_64(ctx, sh, steps, payload):
     ev[1].record(stream)
     ctx.sync(sh)
     unshared_ms = ev[0].elapsed_time(ev[1]) / k
+    mv.close()
+
+    def timed(plan):
+        for _ in range(3):
+            plan.render(True, sh)
+        ctx.sync(sh)
+        ev[0].record(stream)
+        for _ in range(k):
+            plan.render(True, sh)
+        ev[1].record(stream)
+        ctx.sync(sh)
+        return ev[0].elapsed_time(ev[1]) / k
+
+    # the 16 stereo pairs alone (a headset's frames), shared and by look_at
+    eyes = cams[:32]
+    st_mv = MultiView(ctx, cloud, [(c[2], c[3]) for c in eyes], params)
+    st_mv.set_views([cr.make_view(*c) for c in eyes])
+    st_mv.clear(stream=sh)
+    st_best, _ = st_mv.autotune(frames=3, stream=sh)
+    st_pairs = st_mv.shared_pairs()
+    st_ms = timed(st_mv)
+    st_mv.set_views([cr.make_view(*c) for c in workloads.multiview_64(np.array(hdr.min[:]), np.array(hdr.max[:]),
+                                                                      compose_eyes=False)[:32]])
+    st_unshared = st_mv.shared_pairs()
+    st_unshared_ms = timed(st_mv)
+    st_mv.close()
     out = {"points": n, "views": len(cams), "payload": "color" if payload else "index",
            "batched_ms_per_frame": round(mv_ms, 3), "plain_ms_per_frame": round(plain_ms, 3),
            "batched_frames_per_s": round(1e3 / mv_ms, 2), "plain_frames_per_s": round(1e3 / plain_ms, 2),
@@ -619,12 +645,16 @@ def multiview_64(ctx, sh, steps, payload):
            "shared_stereo_pairs": pairs,
            "eyes_by_look_at": {"shared_stereo_pairs": unshared_pairs,
                                "batched_ms_per_frame": round(unshared_ms, 3)},
+           "stereo_32_views": {"shared_stereo_pairs": st_pairs, "batched_ms_per_frame": round(st_ms, 3),
+                               "eyes_by_look_at_pairs": st_unshared,
+                               "eyes_by_look_at_ms_per_frame": round(st_unshared_ms, 3),
+                               "views_per_group": st_best.views_per_group,
+                               "block_threads": st_best.block_threads},
            "autotuned": {"block_threads": best.block_threads, "views_per_group": best.views_per_group,
                          "points_per_thread": 10240 // max(1, best.block_threads)},
            "autotune_ms": report,
            "plain": "64 x cr_render (cull + raster + resolve per view), same stream",
            "batched": "one multi-view plan frame (one cull, one persistent raster, one resolve), CUDA graph"}
-    mv.close()
     for f in fbs:
         f.close()
     cloud.close()

@@ -34,15 +34,16 @@ class Frame(C.Structure):
                 ("files", C.POINTER(FileFrame))]
 
 
-# Where the reference checkout is read from to build the glm probe: the
-# CR_REFERENCE environment variable, else the checkout this build reads from.
-REFERENCE_CHECKOUT = "/root/reference"
-
-
 def reference_dir() -> str:
+    """The reference checkout the probes are compiled from: the CR_REFERENCE
+    environment variable, else a checkout named "reference" beside this
+    repository; "" when neither holds one (the probes are then not built and
+    their tests skip)."""
     import os
-    ref = os.environ.get("CR_REFERENCE") or REFERENCE_CHECKOUT
-    return ref if Path(ref, "libs", "glm", "glm").is_dir() else ""
+    for ref in (os.environ.get("CR_REFERENCE"), str(HERE.parent.parent / "reference")):
+        if ref and Path(ref, "libs", "glm", "glm").is_dir():
+            return ref
+    return ""
 
 
 def build() -> None:

@@ -139,7 +139,8 @@ class LasInfo(C.Structure):
 
 LAZ_MAX_ITEMS = 8
 LAZ_ITEM_BYTE, LAZ_ITEM_POINT10, LAZ_ITEM_GPSTIME11, LAZ_ITEM_RGB12 = 0, 6, 7, 8
-LAZ_POINTWISE, LAZ_POINTWISE_CHUNKED = 1, 2
+LAZ_ITEM_POINT14, LAZ_ITEM_RGB14, LAZ_ITEM_RGBNIR14, LAZ_ITEM_BYTE14 = 10, 11, 12, 14
+LAZ_POINTWISE, LAZ_POINTWISE_CHUNKED, LAZ_LAYERED_CHUNKED = 1, 2, 3
 LAZ_DEFAULT_CHUNK, LAZ_VARIABLE_CHUNKS = 50000, -1
 
 

@@ -589,7 +589,10 @@ struct Point10 {
 // GPSTIME11 (8-byte double, coded as its 64-bit pattern): up to four
 // interleaved time sequences, each with its last value and last 32-bit delta;
 // a delta is coded as a rounded multiple of the last delta plus a corrector,
-// a jump to another sequence, or a full 64-bit value.
+// a jump to another sequence, or a full 64-bit value.  The layered POINT14
+// coder (lasreaditemcompressed_v3.cpp read_gps_time) uses the same scheme
+// without the "unchanged" symbols (its change flag rides with the point):
+// 5 and 515 symbols, full value at 1 and 511.
 constexpr uint32_t kGpsMulti = 500, kGpsUnchanged = 511, kGpsFull = 512, kGpsSymbols = 516;
 constexpr int32_t kGpsMinus = -10;
 
@@ -599,20 +602,25 @@ struct GpsTime11 {
     uint64_t t[4];
     int32_t diff[4], extreme[4];
     uint32_t last, next;
+    uint32_t zd_diff, zd_full, m_full;  // symbol layout: point-wise or layered
 
-    explicit GpsTime11(bool dec) {
-        multi.create(kGpsSymbols, dec);
-        zero_diff.create(6, dec);
+    explicit GpsTime11(bool dec, bool layered = false) {
+        multi.create(layered ? kGpsSymbols - 1 : kGpsSymbols, dec);
+        zero_diff.create(layered ? 5 : 6, dec);
         ic.create(32, 9, dec);
+        zd_diff = layered ? 0 : 1;
+        zd_full = layered ? 1 : 2;
+        m_full = layered ? kGpsFull - 1 : kGpsFull;
     }
-    void init(const uint8_t* item) {
+    void init_time(uint64_t t0) {
         last = next = 0;
         for (int i = 0; i < 4; i++) diff[i] = extreme[i] = 0, t[i] = 0;
-        t[0] = ld64(item);
+        t[0] = t0;
         multi.reset();
         zero_diff.reset();
         ic.reset();
     }
+    void init(const uint8_t* item) { init_time(ld64(item)); }
     static int32_t times(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
     void count_extreme(int32_t g) {
         if (++extreme[last] > 3) {
@@ -628,18 +636,19 @@ struct GpsTime11 {
         diff[last] = 0;
         extreme[last] = 0;
     }
-    void decode(Decoder& d, uint8_t* item) {
+    // one time value into t[last]
+    void decode_time(Decoder& d) {
         for (;;) {
             if (diff[last] == 0) {
                 const uint32_t s = d.sym(zero_diff);
-                if (s == 1) {
+                if (s == zd_diff) {
                     diff[last] = ic.decode(d, 0, 0);
                     t[last] += (uint64_t)(int64_t)diff[last];
                     extreme[last] = 0;
-                } else if (s == 2) {
+                } else if (s == zd_full) {
                     decode_full(d);
-                } else if (s > 2) {
-                    last = (last + s - 2) & 3;
+                } else if (s > zd_full) {
+                    last = (last + s - zd_full) & 3;
                     continue;
                 }
             } else {
@@ -667,15 +676,18 @@ struct GpsTime11 {
                         }
                     }
                     t[last] += (uint64_t)(int64_t)g;
-                } else if (s == kGpsFull) {
+                } else if (s == m_full) {
                     decode_full(d);
-                } else if (s > kGpsFull) {
-                    last = (last + s - kGpsFull) & 3;
+                } else if (s > m_full) {
+                    last = (last + s - m_full) & 3;
                     continue;
                 }
             }
             break;
         }
+    }
+    void decode(Decoder& d, uint8_t* item) {
+        decode_time(d);
         st64(item, t[last]);
     }
     // float ratio of the deltas rounded half away from zero (I32_QUANTIZE);
@@ -783,6 +795,45 @@ struct GpsTime11 {
 // RGB12 (three 16-bit channels): a 7-bit mask of which bytes changed (bit 6:
 // the channels differ from each other); green and blue bytes are predicted
 // from red's change (lasreaditemcompressed_v2.cpp RGB12).
+// The channels of one RGB value from the previous one `last` (RGB12 v2, and
+// per scanner channel the RGB14 / RGBNIR14 v3 layers).
+void rgb_decode(Decoder& d, SymModel& used, SymModel* diff, const uint16_t* last, uint16_t* v) {
+    const uint32_t s = d.sym(used);
+    v[0] = (s & 1) ? (uint16_t)fold8((int32_t)d.sym(diff[0]) + (last[0] & 255)) : (uint16_t)(last[0] & 0xFF);
+    if (s & 2)
+        v[0] |= (uint16_t)(fold8((int32_t)d.sym(diff[1]) + (last[0] >> 8)) << 8);
+    else
+        v[0] |= (uint16_t)(last[0] & 0xFF00);
+    if (s & 64) {
+        int32_t dl = (v[0] & 0xFF) - (last[0] & 0xFF);
+        if (s & 4)
+            v[1] = (uint16_t)fold8((int32_t)d.sym(diff[2]) + clamp8(dl + (last[1] & 255)));
+        else
+            v[1] = (uint16_t)(last[1] & 0xFF);
+        if (s & 16) {
+            const int32_t c = (int32_t)d.sym(diff[4]);
+            dl = (dl + ((v[1] & 0xFF) - (last[1] & 0xFF))) / 2;
+            v[2] = (uint16_t)fold8(c + clamp8(dl + (last[2] & 255)));
+        } else {
+            v[2] = (uint16_t)(last[2] & 0xFF);
+        }
+        int32_t dh = (v[0] >> 8) - (last[0] >> 8);
+        if (s & 8)
+            v[1] |= (uint16_t)(fold8((int32_t)d.sym(diff[3]) + clamp8(dh + (last[1] >> 8))) << 8);
+        else
+            v[1] |= (uint16_t)(last[1] & 0xFF00);
+        if (s & 32) {
+            const int32_t c = (int32_t)d.sym(diff[5]);
+            dh = (dh + ((v[1] >> 8) - (last[1] >> 8))) / 2;
+            v[2] |= (uint16_t)(fold8(c + clamp8(dh + (last[2] >> 8))) << 8);
+        } else {
+            v[2] |= (uint16_t)(last[2] & 0xFF00);
+        }
+    } else {
+        v[1] = v[2] = v[0];
+    }
+}
+
 struct Rgb12 {
     SymModel used, diff[6];
     uint16_t last[3];
@@ -797,40 +848,7 @@ struct Rgb12 {
     }
     void decode(Decoder& d, uint8_t* item) {
         uint16_t v[3];
-        const uint32_t s = d.sym(used);
-        v[0] = (s & 1) ? (uint16_t)fold8((int32_t)d.sym(diff[0]) + (last[0] & 255)) : (uint16_t)(last[0] & 0xFF);
-        if (s & 2)
-            v[0] |= (uint16_t)(fold8((int32_t)d.sym(diff[1]) + (last[0] >> 8)) << 8);
-        else
-            v[0] |= (uint16_t)(last[0] & 0xFF00);
-        if (s & 64) {
-            int32_t dl = (v[0] & 0xFF) - (last[0] & 0xFF);
-            if (s & 4)
-                v[1] = (uint16_t)fold8((int32_t)d.sym(diff[2]) + clamp8(dl + (last[1] & 255)));
-            else
-                v[1] = (uint16_t)(last[1] & 0xFF);
-            if (s & 16) {
-                const int32_t c = (int32_t)d.sym(diff[4]);
-                dl = (dl + ((v[1] & 0xFF) - (last[1] & 0xFF))) / 2;
-                v[2] = (uint16_t)fold8(c + clamp8(dl + (last[2] & 255)));
-            } else {
-                v[2] = (uint16_t)(last[2] & 0xFF);
-            }
-            int32_t dh = (v[0] >> 8) - (last[0] >> 8);
-            if (s & 8)
-                v[1] |= (uint16_t)(fold8((int32_t)d.sym(diff[3]) + clamp8(dh + (last[1] >> 8))) << 8);
-            else
-                v[1] |= (uint16_t)(last[1] & 0xFF00);
-            if (s & 32) {
-                const int32_t c = (int32_t)d.sym(diff[5]);
-                dh = (dh + ((v[1] >> 8) - (last[1] >> 8))) / 2;
-                v[2] |= (uint16_t)(fold8(c + clamp8(dh + (last[2] >> 8))) << 8);
-            } else {
-                v[2] |= (uint16_t)(last[2] & 0xFF00);
-            }
-        } else {
-            v[1] = v[2] = v[0];
-        }
+        rgb_decode(d, used, diff, last, v);
         for (int c = 0; c < 3; c++) {
             last[c] = v[c];
             st16(item + 2 * c, v[c]);
@@ -895,6 +913,397 @@ struct Bytes {
     }
 };
 
+// ---- layered items of LAS 1.4 points, version 3 (lasreaditemcompressed_v3.cpp)
+//
+// A layered chunk holds, after its raw first point, the point count and the
+// byte size of every layer, then the layers: each attribute group has its own
+// coder run, so a group that never changes in the chunk costs no bytes.
+// Every item keeps one prediction context per scanner channel.  As in LASzip
+// 3.4's version 3 items, the channel the POINT14 item hands the other items
+// is the new channel on a point that switches channels and 0 on every other
+// point, and an item switching to a context it already used keeps reading the
+// previous context's last values: the bytes of such files follow that rule.
+
+// number_return_map_6ctx of laszip_common_v3.hpp: [number of returns][return]
+const uint8_t kReturnMap6[16][16] = {
+    {0, 1, 2, 3, 4, 5, 3, 4, 4, 5, 5, 5, 5, 5, 5, 5}, {1, 0, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3},
+    {2, 1, 2, 4, 4, 4, 4, 4, 4, 4, 4, 3, 3, 3, 3, 3}, {3, 3, 4, 5, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4},
+    {4, 3, 4, 4, 5, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4}, {5, 3, 4, 4, 4, 5, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4},
+    {3, 3, 4, 4, 4, 4, 5, 4, 4, 4, 4, 4, 4, 4, 4, 4}, {4, 3, 4, 4, 4, 4, 4, 5, 4, 4, 4, 4, 4, 4, 4, 4},
+    {4, 3, 4, 4, 4, 4, 4, 4, 5, 4, 4, 4, 4, 4, 4, 4}, {5, 3, 4, 4, 4, 4, 4, 4, 4, 5, 4, 4, 4, 4, 4, 4},
+    {5, 3, 4, 4, 4, 4, 4, 4, 4, 4, 5, 4, 4, 4, 4, 4}, {5, 3, 3, 4, 4, 4, 4, 4, 4, 4, 4, 5, 5, 4, 4, 4},
+    {5, 3, 3, 4, 4, 4, 4, 4, 4, 4, 4, 5, 5, 5, 4, 4}, {5, 3, 3, 4, 4, 4, 4, 4, 4, 4, 4, 4, 5, 5, 5, 4},
+    {5, 3, 3, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 5, 5, 5}, {5, 3, 3, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 5, 5}};
+// number_return_level_8ctx: |n - r| capped at 7
+inline uint32_t return_level8(uint32_t n, uint32_t r) { return std::min(n > r ? n - r : r - n, 7u); }
+
+// Models of one byte-valued context table, created on first use and reset on
+// first use after their owner's context was (re)initialised (generation).
+struct ModelBank {
+    uint32_t symbols = 0;
+    std::vector<std::unique_ptr<SymModel>> m;
+    std::vector<uint32_t> gen;
+    void create(uint32_t count, uint32_t syms) {
+        symbols = syms;
+        m.resize(count);
+        gen.assign(count, 0);
+    }
+    SymModel& get(uint32_t i, uint32_t g) {
+        if (!m[i]) {
+            m[i].reset(new SymModel());
+            m[i]->create(symbols, true);
+        }
+        if (gen[i] != g) {
+            gen[i] = g;
+            m[i]->reset();
+        }
+        return *m[i];
+    }
+};
+
+// The 30-byte LAS 1.4 point record (formats 6-10).
+struct Point14 {
+    int32_t X, Y, Z;
+    uint16_t intensity;
+    uint32_t r, n, cflags, channel, sdir, edge, cls, user;
+    int16_t scan_angle;
+    uint16_t source;
+    uint64_t gps;
+    bool gps_change;
+    void load(const uint8_t* p) {
+        X = ld32s(p);
+        Y = ld32s(p + 4);
+        Z = ld32s(p + 8);
+        intensity = ld16(p + 12);
+        r = p[14] & 15u;
+        n = p[14] >> 4;
+        cflags = p[15] & 15u;
+        channel = (p[15] >> 4) & 3u;
+        sdir = (p[15] >> 6) & 1u;
+        edge = p[15] >> 7;
+        cls = p[16];
+        user = p[17];
+        scan_angle = (int16_t)ld16(p + 18);
+        source = ld16(p + 20);
+        gps = ld64(p + 22);
+        gps_change = false;
+    }
+    void store(uint8_t* p) const {
+        st32(p, (uint32_t)X);
+        st32(p + 4, (uint32_t)Y);
+        st32(p + 8, (uint32_t)Z);
+        st16(p + 12, intensity);
+        p[14] = (uint8_t)(r | (n << 4));
+        p[15] = (uint8_t)(cflags | (channel << 4) | (sdir << 6) | (edge << 7));
+        p[16] = (uint8_t)cls;
+        p[17] = (uint8_t)user;
+        st16(p + 18, (uint16_t)scan_angle);
+        st16(p + 20, source);
+        st64(p + 22, gps);
+    }
+};
+
+// POINT14 layers, in stream order
+enum { kLayerXY, kLayerZ, kLayerClass, kLayerFlags, kLayerIntensity, kLayerScanAngle, kLayerUser,
+       kLayerSource, kLayerGps, kP14Layers };
+
+// One scanner channel's POINT14 prediction state (createAndInitModelsAndDecompressors).
+struct P14Context {
+    bool used = false;
+    uint32_t gen = 0;
+    Point14 last;
+    uint16_t last_intensity[8];
+    int32_t last_Z[8];
+    Median5 mx[12], my[12];
+    SymModel changed[8], channel, rnum_gps_same;
+    ModelBank nret, rnum, cls, flags, user;
+    IntCoder ic_dx, ic_dy, ic_z, ic_intensity, ic_scan_angle, ic_source;
+    GpsTime11 gps{true, true};
+
+    P14Context() {
+        for (auto& m : changed) m.create(128, true);
+        channel.create(3, true);
+        rnum_gps_same.create(13, true);
+        nret.create(16, 16);
+        rnum.create(16, 16);
+        cls.create(64, 256);
+        flags.create(64, 64);
+        user.create(64, 256);
+        ic_dx.create(32, 2, true);
+        ic_dy.create(32, 22, true);
+        ic_z.create(32, 20, true);
+        ic_intensity.create(16, 4, true);
+        ic_scan_angle.create(16, 2, true);
+        ic_source.create(16, 1, true);
+    }
+    void init(const Point14& p, uint32_t chunk_gen) {
+        gen = chunk_gen;
+        for (auto& m : changed) m.reset();
+        channel.reset();
+        rnum_gps_same.reset();
+        ic_dx.reset();
+        ic_dy.reset();
+        ic_z.reset();
+        ic_intensity.reset();
+        ic_scan_angle.reset();
+        ic_source.reset();
+        for (int i = 0; i < 12; i++) {
+            mx[i].reset();
+            my[i].reset();
+        }
+        for (int i = 0; i < 8; i++) {
+            last_Z[i] = p.Z;
+            last_intensity[i] = p.intensity;
+        }
+        gps.init_time(p.gps);
+        last = p;
+        last.gps_change = false;
+        used = true;
+    }
+};
+
+struct Point14Layered {
+    std::unique_ptr<P14Context> ctx[4];
+    uint32_t cur = 0, gen = 0;
+    Decoder d[kP14Layers];
+    bool changed[kP14Layers];
+
+    P14Context& context(uint32_t c) {
+        if (!ctx[c]) ctx[c].reset(new P14Context());
+        return *ctx[c];
+    }
+    // chunk start: every context unused; the first point's channel current
+    void init(const uint8_t* item, uint32_t& shared) {
+        for (auto& c : ctx)
+            if (c) c->used = false;
+        Point14 p;
+        p.load(item);
+        cur = p.channel;
+        shared = cur;
+        context(cur).init(p, ++gen);
+    }
+    void decode(uint8_t* item, uint32_t& shared) {
+        P14Context* c = &context(cur);
+        Decoder& dx = d[kLayerXY];
+        uint32_t lpr = (c->last.r == 1 ? 1u : 0u) + (c->last.r >= c->last.n ? 2u : 0u) +
+                       (c->last.gps_change ? 4u : 0u);
+        const uint32_t cv = dx.sym(c->changed[lpr]);
+        if (cv & (1u << 6)) {  // the scanner channel changed
+            const uint32_t sc = (cur + dx.sym(c->channel) + 1) % 4;
+            P14Context& nc = context(sc);
+            if (!nc.used) nc.init(c->last, ++gen);
+            cur = sc;
+            shared = cur;
+            c = &nc;
+            c->last.channel = sc;
+        }
+        Point14& L = c->last;
+        const bool source_change = (cv & (1u << 5)) != 0;
+        const uint32_t gps_change = (cv >> 4) & 1u;
+        const bool angle_change = (cv & (1u << 3)) != 0;
+        const uint32_t last_n = L.n, last_r = L.r;
+        uint32_t n = last_n, r = last_r;
+        if (cv & (1u << 2)) {
+            n = dx.sym(c->nret.get(last_n, c->gen));
+            L.n = n;
+        }
+        switch (cv & 3u) {
+            case 0: break;
+            case 1: r = (last_r + 1) % 16; break;
+            case 2: r = (last_r + 15) % 16; break;
+            default:
+                if (gps_change) r = dx.sym(c->rnum.get(last_r, c->gen));
+                else r = (last_r + dx.sym(c->rnum_gps_same) + 2) % 16;
+                break;
+        }
+        L.r = r;
+        const uint32_t m = kReturnMap6[n][r], l = return_level8(n, r);
+        const uint32_t cpr = (r == 1 ? 2u : 0u) + (r >= n ? 1u : 0u);
+        const uint32_t one = n == 1;
+        const uint32_t mi = (m << 1) | gps_change;
+        const int32_t ddx = c->ic_dx.decode(dx, c->mx[mi].get(), one);
+        L.X = (int32_t)((uint32_t)L.X + (uint32_t)ddx);
+        c->mx[mi].add(ddx);
+        const uint32_t kx = c->ic_dx.k;
+        const int32_t ddy = c->ic_dy.decode(dx, c->my[mi].get(), one + (kx < 20 ? kx & ~1u : 20));
+        L.Y = (int32_t)((uint32_t)L.Y + (uint32_t)ddy);
+        c->my[mi].add(ddy);
+        if (changed[kLayerZ]) {
+            const uint32_t kz = (c->ic_dx.k + c->ic_dy.k) / 2;
+            L.Z = c->ic_z.decode(d[kLayerZ], c->last_Z[l], one + (kz < 18 ? kz & ~1u : 18));
+            c->last_Z[l] = L.Z;
+        }
+        if (changed[kLayerClass]) {
+            const uint32_t ccc = ((L.cls & 31u) << 1) + (cpr == 3 ? 1u : 0u);
+            L.cls = d[kLayerClass].sym(c->cls.get(ccc, c->gen));
+        }
+        if (changed[kLayerFlags]) {
+            const uint32_t lf = (L.edge << 5) | (L.sdir << 4) | L.cflags;
+            const uint32_t f = d[kLayerFlags].sym(c->flags.get(lf, c->gen));
+            L.edge = (f >> 5) & 1u;
+            L.sdir = (f >> 4) & 1u;
+            L.cflags = f & 15u;
+        }
+        if (changed[kLayerIntensity]) {
+            const uint32_t ii = (cpr << 1) | gps_change;
+            const uint16_t v = (uint16_t)c->ic_intensity.decode(d[kLayerIntensity], c->last_intensity[ii], cpr);
+            c->last_intensity[ii] = v;
+            L.intensity = v;
+        }
+        if (changed[kLayerScanAngle] && angle_change)
+            L.scan_angle = (int16_t)c->ic_scan_angle.decode(d[kLayerScanAngle], L.scan_angle, gps_change);
+        if (changed[kLayerUser]) L.user = d[kLayerUser].sym(c->user.get(L.user / 4, c->gen));
+        if (changed[kLayerSource] && source_change)
+            L.source = (uint16_t)c->ic_source.decode(d[kLayerSource], L.source, 0);
+        if (changed[kLayerGps] && gps_change) {
+            c->gps.decode_time(d[kLayerGps]);
+            L.gps = c->gps.t[c->gps.last];
+        }
+        L.store(item);
+        L.gps_change = gps_change != 0;
+    }
+};
+
+// RGB14 / RGBNIR14 per scanner channel: the RGB12 predictor (and a two-byte
+// NIR channel) with the item's own layers.
+struct RgbCtx {
+    bool used = false;
+    SymModel used_m, diff[6], nir_used, nir_diff[2];
+    uint16_t last[4];
+    explicit RgbCtx(bool nir) {
+        used_m.create(128, true);
+        for (auto& m : diff) m.create(256, true);
+        if (nir) {
+            nir_used.create(4, true);
+            nir_diff[0].create(256, true);
+            nir_diff[1].create(256, true);
+        }
+    }
+    void init(const uint16_t* item, bool nir) {
+        used_m.reset();
+        for (auto& m : diff) m.reset();
+        if (nir) {
+            nir_used.reset();
+            nir_diff[0].reset();
+            nir_diff[1].reset();
+        }
+        for (int c = 0; c < (nir ? 4 : 3); c++) last[c] = item[c];
+        used = true;
+    }
+};
+
+struct Rgb14Layered {
+    bool nir;
+    std::unique_ptr<RgbCtx> ctx[4];
+    uint32_t cur = 0;
+    Decoder d[2];  // RGB, NIR
+    bool changed[2];
+    explicit Rgb14Layered(bool with_nir) : nir(with_nir) {}
+
+    RgbCtx& context(uint32_t c) {
+        if (!ctx[c]) ctx[c].reset(new RgbCtx(nir));
+        return *ctx[c];
+    }
+    void init(const uint8_t* item, uint32_t shared) {
+        for (auto& c : ctx)
+            if (c) c->used = false;
+        uint16_t v[4];
+        for (int c = 0; c < (nir ? 4 : 3); c++) v[c] = ld16(item + 2 * c);
+        cur = shared;
+        context(cur).init(v, nir);
+    }
+    void decode(uint8_t* item, uint32_t shared) {
+        uint16_t* last = context(cur).last;
+        if (cur != shared) {
+            cur = shared;
+            RgbCtx& nc = context(cur);
+            if (!nc.used) {
+                nc.init(last, nir);
+                last = nc.last;
+            }
+        }
+        RgbCtx& c = context(cur);
+        uint16_t v[3];
+        if (changed[0]) {
+            rgb_decode(d[0], c.used_m, c.diff, last, v);
+            for (int k = 0; k < 3; k++) last[k] = v[k];
+        } else {
+            for (int k = 0; k < 3; k++) v[k] = last[k];
+        }
+        for (int k = 0; k < 3; k++) st16(item + 2 * k, v[k]);
+        if (!nir) return;
+        uint16_t w;
+        if (changed[1]) {
+            const uint32_t s = d[1].sym(c.nir_used);
+            w = (s & 1) ? (uint16_t)fold8((int32_t)d[1].sym(c.nir_diff[0]) + (last[3] & 255))
+                        : (uint16_t)(last[3] & 0xFF);
+            if (s & 2)
+                w |= (uint16_t)(fold8((int32_t)d[1].sym(c.nir_diff[1]) + (last[3] >> 8)) << 8);
+            else
+                w |= (uint16_t)(last[3] & 0xFF00);
+            last[3] = w;
+        } else {
+            w = last[3];
+        }
+        st16(item + 6, w);
+    }
+};
+
+// BYTE14: every extra byte its own layer and, per channel, its own model.
+struct BytesCtx {
+    bool used = false;
+    std::vector<SymModel> m;
+    std::vector<uint8_t> last;
+    explicit BytesCtx(uint32_t count) : m(count), last(count) {
+        for (auto& x : m) x.create(256, true);
+    }
+};
+
+struct Bytes14Layered {
+    uint32_t count;
+    std::unique_ptr<BytesCtx> ctx[4];
+    uint32_t cur = 0;
+    std::vector<Decoder> d;
+    std::vector<uint8_t> changed;
+    explicit Bytes14Layered(uint32_t n) : count(n), d(n), changed(n) {}
+
+    BytesCtx& context(uint32_t c) {
+        if (!ctx[c]) ctx[c].reset(new BytesCtx(count));
+        return *ctx[c];
+    }
+    void init_context(BytesCtx& c, const uint8_t* item) {
+        for (auto& x : c.m) x.reset();
+        std::memcpy(c.last.data(), item, count);
+        c.used = true;
+    }
+    void init(const uint8_t* item, uint32_t shared) {
+        for (auto& c : ctx)
+            if (c) c->used = false;
+        cur = shared;
+        init_context(context(cur), item);
+    }
+    void decode(uint8_t* item, uint32_t shared) {
+        uint8_t* last = context(cur).last.data();
+        if (cur != shared) {
+            cur = shared;
+            BytesCtx& nc = context(cur);
+            if (!nc.used) {
+                init_context(nc, last);
+                last = nc.last.data();
+            }
+        }
+        BytesCtx& c = context(cur);
+        for (uint32_t i = 0; i < count; i++) {
+            if (changed[i]) {
+                item[i] = (uint8_t)fold8(last[i] + (int32_t)d[i].sym(c.m[i]));
+                last[i] = item[i];
+            } else {
+                item[i] = last[i];
+            }
+        }
+    }
+};
+
 // ---- point layouts and one thread's chunk codec ----------------------------
 
 struct Item {
@@ -904,7 +1313,8 @@ struct Item {
 struct Layout {
     std::vector<Item> items;
     int32_t bpp = 0;
-    int32_t rgb_offset = -1;  // of the RGB12 item in a record, -1 without one
+    int32_t rgb_offset = -1;  // of the RGB12 / RGB14 / RGBNIR14 item in a record, -1 without one
+    bool layered = false;     // LAS 1.4 items (compressor 3)
 };
 
 // Items of LAS point formats 0-3 plus extra bytes (laszip.cpp setup).
@@ -935,6 +1345,10 @@ class PointCodec {
                 case CR_LAZ_ITEM_POINT10: p10_.reset(new Point10(decoder)); break;
                 case CR_LAZ_ITEM_GPSTIME11: gps_.reset(new GpsTime11(decoder)); break;
                 case CR_LAZ_ITEM_RGB12: rgb_.reset(new Rgb12(decoder)); break;
+                case CR_LAZ_ITEM_POINT14: p14_.reset(new Point14Layered()); break;
+                case CR_LAZ_ITEM_RGB14: rgb14_.reset(new Rgb14Layered(false)); break;
+                case CR_LAZ_ITEM_RGBNIR14: rgb14_.reset(new Rgb14Layered(true)); break;
+                case CR_LAZ_ITEM_BYTE14: bytes14_.reset(new Bytes14Layered((uint32_t)it.size)); break;
                 default: bytes_.reset(new Bytes((uint32_t)it.size, decoder)); break;
             }
         }
@@ -950,6 +1364,7 @@ class PointCodec {
             *end = src;
             return true;
         }
+        if (layout_.layered) return decode_layered(src, file_end, skip, take, stop, out, end);
         const int64_t bpp = layout_.bpp;
         if (file_end - src < bpp) return false;
         uint8_t* rec = rec_.data();
@@ -1005,6 +1420,82 @@ class PointCodec {
     }
 
   private:
+    // lasreadpoint.cpp read() for layered chunks: the raw first point, the
+    // point count, every item's layer sizes, then every item's layers.
+    bool decode_layered(const uint8_t* src, const uint8_t* file_end, int64_t skip, int64_t take,
+                        int64_t stop, uint8_t* out, const uint8_t** end) {
+        const int64_t bpp = layout_.bpp;
+        if (file_end - src < bpp + 4) return false;
+        uint8_t* rec = rec_.data();
+        std::memcpy(rec, src, (size_t)bpp);
+        const uint8_t* q = src + bpp + 4;  // the stored point count is not needed
+        std::vector<uint32_t>& sizes = sizes_;
+        sizes.clear();
+        for (const Item& it : layout_.items) {
+            const int nl = it.type == CR_LAZ_ITEM_POINT14 ? kP14Layers
+                           : it.type == CR_LAZ_ITEM_RGBNIR14 ? 2
+                           : it.type == CR_LAZ_ITEM_RGB14 ? 1 : it.size;
+            for (int k = 0; k < nl; k++) {
+                if (file_end - q < 4) return false;
+                sizes.push_back(ld32(q));
+                q += 4;
+            }
+        }
+        size_t li = 0;
+        const uint8_t* at = q;
+        auto layer = [&](Decoder& d, bool always) -> bool {  // one layer's bytes; false: empty
+            const uint32_t n = sizes[li++];
+            d.p = at;
+            d.end = at + n;
+            d.bad = (int64_t)n > file_end - at;
+            at += n;
+            if (n == 0 && !always) return false;
+            d.start();
+            return true;
+        };
+        for (const Item& it : layout_.items) {
+            if (it.type == CR_LAZ_ITEM_POINT14) {
+                for (int k = 0; k < kP14Layers; k++) p14_->changed[k] = layer(p14_->d[k], k == kLayerXY);
+            } else if (it.type == CR_LAZ_ITEM_RGB14) {
+                rgb14_->changed[0] = layer(rgb14_->d[0], false);
+            } else if (it.type == CR_LAZ_ITEM_RGBNIR14) {
+                rgb14_->changed[0] = layer(rgb14_->d[0], false);
+                rgb14_->changed[1] = layer(rgb14_->d[1], false);
+            } else {
+                for (int k = 0; k < it.size; k++) bytes14_->changed[k] = layer(bytes14_->d[k], false);
+            }
+        }
+        if (at > file_end) return false;
+        // POINT14 comes first and hands its scanner channel to the others
+        uint32_t shared = 0;
+        size_t off = 0;
+        for (const Item& it : layout_.items) {
+            if (it.type == CR_LAZ_ITEM_POINT14) p14_->init(rec + off, shared);
+            else if (it.type == CR_LAZ_ITEM_BYTE14) bytes14_->init(rec + off, shared);
+            else rgb14_->init(rec + off, shared);
+            off += (size_t)it.size;
+        }
+        if (skip == 0 && take > 0) std::memcpy(out, rec, (size_t)bpp);
+        for (int64_t i = 1; i < stop; i++) {
+            shared = 0;  // lasreadpoint.cpp read(): a fresh context per point
+            off = 0;
+            for (const Item& it : layout_.items) {
+                if (it.type == CR_LAZ_ITEM_POINT14) p14_->decode(rec + off, shared);
+                else if (it.type == CR_LAZ_ITEM_BYTE14) bytes14_->decode(rec + off, shared);
+                else rgb14_->decode(rec + off, shared);
+                off += (size_t)it.size;
+            }
+            if (i >= skip && i < take) std::memcpy(out + (i - skip) * bpp, rec, (size_t)bpp);
+        }
+        *end = at;
+        bool bad = false;
+        for (const Decoder& d : p14_->d) bad |= d.bad;
+        if (rgb14_) bad |= rgb14_->d[0].bad || rgb14_->d[1].bad;
+        if (bytes14_)
+            for (const Decoder& d : bytes14_->d) bad |= d.bad;
+        return !bad;
+    }
+
     void init_items(const uint8_t* rec) {
         ++chunk_no_;
         size_t off = 0;
@@ -1026,6 +1517,10 @@ class PointCodec {
     std::unique_ptr<GpsTime11> gps_;
     std::unique_ptr<Rgb12> rgb_;
     std::unique_ptr<Bytes> bytes_;
+    std::unique_ptr<Point14Layered> p14_;
+    std::unique_ptr<Rgb14Layered> rgb14_;
+    std::unique_ptr<Bytes14Layered> bytes14_;
+    std::vector<uint32_t> sizes_;
 };
 
 int resolve_threads(int32_t threads, int64_t work) {
@@ -1125,7 +1620,7 @@ cr_status decode_range(const cr_laz* z, int64_t first, int64_t n, uint8_t* out, 
     const int64_t c1 = (int64_t)(std::upper_bound(cf.begin(), cf.end(), first + n - 1) - cf.begin()) - 1;
     std::atomic<int64_t> next(c0);
     std::atomic<int> status(CR_OK);
-    const bool check_end = z->info.compressor == CR_LAZ_POINTWISE_CHUNKED;
+    const bool check_end = z->info.compressor != CR_LAZ_POINTWISE;
     run_workers(resolve_threads(threads, c1 - c0 + 1), [&](int) {
         PointCodec codec(z->layout, true);
         for (int64_t c = next++; c <= c1 && status.load() == CR_OK; c = next++) {
@@ -1186,27 +1681,43 @@ cr_status cr_laz_open(const void* file, int64_t size, cr_laz** out, cr_laz_info*
     z->info.num_items = num_items;
     Layout& L = z->layout;
     int32_t off = 0;
-    bool seen[9] = {false};
+    bool seen[16] = {false};
     for (int32_t i = 0; i < num_items; i++) {
         const Item it{ld16(vlr + 34 + 6 * i), ld16(vlr + 36 + 6 * i), ld16(vlr + 38 + 6 * i)};
         z->info.item_type[i] = it.type;
         z->info.item_size[i] = it.size;
         z->info.item_version[i] = it.version;
-        const bool known = (it.type == CR_LAZ_ITEM_POINT10 && it.size == 20) ||
-                           (it.type == CR_LAZ_ITEM_GPSTIME11 && it.size == 8) ||
-                           (it.type == CR_LAZ_ITEM_RGB12 && it.size == 6) ||
-                           (it.type == CR_LAZ_ITEM_BYTE && it.size >= 1);
-        if (!known || it.version != 2) st = CR_ERR_UNSUPPORTED;
+        const bool v2 = (it.type == CR_LAZ_ITEM_POINT10 && it.size == 20) ||
+                        (it.type == CR_LAZ_ITEM_GPSTIME11 && it.size == 8) ||
+                        (it.type == CR_LAZ_ITEM_RGB12 && it.size == 6) ||
+                        (it.type == CR_LAZ_ITEM_BYTE && it.size >= 1);
+        const bool v3 = (it.type == CR_LAZ_ITEM_POINT14 && it.size == 30) ||
+                        (it.type == CR_LAZ_ITEM_RGB14 && it.size == 6) ||
+                        (it.type == CR_LAZ_ITEM_RGBNIR14 && it.size == 8) ||
+                        (it.type == CR_LAZ_ITEM_BYTE14 && it.size >= 1);
+        if (!(v2 && it.version == 2) && !(v3 && it.version == 3)) st = CR_ERR_UNSUPPORTED;
         else if (seen[it.type]) st = CR_ERR_INVALID_ARG;
         else seen[it.type] = true;
-        if (it.type == CR_LAZ_ITEM_RGB12) L.rgb_offset = off;
+        if (it.type == CR_LAZ_ITEM_RGB12 || it.type == CR_LAZ_ITEM_RGB14 || it.type == CR_LAZ_ITEM_RGBNIR14)
+            L.rgb_offset = off;
+        if (v3) L.layered = true;
         L.items.push_back(it);
         off += it.size;
     }
-    if (compressor != CR_LAZ_POINTWISE && compressor != CR_LAZ_POINTWISE_CHUNKED) return CR_ERR_UNSUPPORTED;
+    if (compressor != CR_LAZ_POINTWISE && compressor != CR_LAZ_POINTWISE_CHUNKED &&
+        compressor != CR_LAZ_LAYERED_CHUNKED)
+        return CR_ERR_UNSUPPORTED;
     if (coder != 0) return CR_ERR_UNSUPPORTED;
     if (st != CR_OK) return st;
-    if (!seen[CR_LAZ_ITEM_POINT10] || off != z->info.las.bytes_per_point) return CR_ERR_INVALID_ARG;
+    if (off != z->info.las.bytes_per_point) return CR_ERR_INVALID_ARG;
+    if (L.layered) {  // LAS 1.4 items: layered chunks, POINT14 first, no point-wise items
+        if (compressor != CR_LAZ_LAYERED_CHUNKED || L.items[0].type != CR_LAZ_ITEM_POINT14 ||
+            seen[CR_LAZ_ITEM_POINT10] || seen[CR_LAZ_ITEM_GPSTIME11] || seen[CR_LAZ_ITEM_RGB12] ||
+            seen[CR_LAZ_ITEM_BYTE] || (seen[CR_LAZ_ITEM_RGB14] && seen[CR_LAZ_ITEM_RGBNIR14]))
+            return CR_ERR_INVALID_ARG;
+    } else if (!seen[CR_LAZ_ITEM_POINT10] || compressor == CR_LAZ_LAYERED_CHUNKED) {
+        return CR_ERR_INVALID_ARG;
+    }
     L.bpp = off;
     const int64_t n = z->info.las.num_points;
     if (points_at < pos || points_at > size) return CR_ERR_INVALID_ARG;

@@ -17,12 +17,15 @@
  * exactly as cr_cloud_load_las encodes the same records, except that point
  * formats without RGB get colour 0, as LASzip's zeroed rgb gives loadLaz.
  *
- * Supported streams: the LASzip point-wise coders, chunked (compressor 2, the
- * default for point formats 0-5, fixed or variable chunk sizes) or not
- * (compressor 1), with version-2 items POINT10, GPSTIME11, RGB12 and BYTE
- * (extra bytes): LAS point formats 0-3 as LASzip 2.x and 3.x write them.
- * The layered coder of LAS 1.4 point formats 6-10 (compressor 3, items
- * version 3/4) and version-1 items return CR_ERR_UNSUPPORTED.
+ * Supported streams (decoding): the LASzip point-wise coders, chunked
+ * (compressor 2, the default for point formats 0-5, fixed or variable chunk
+ * sizes) or not (compressor 1), with version-2 items POINT10, GPSTIME11,
+ * RGB12 and BYTE (LAS point formats 0-3 plus extra bytes); and the layered
+ * coder of LAS 1.4 (compressor 3) with version-3 items POINT14, RGB14,
+ * RGBNIR14 and BYTE14 (point formats 6, 7 and 8 plus extra bytes), as
+ * LASzip 3.4 writes them.  Version-1 and version-4 items and wave packets
+ * (formats 4, 5, 9, 10) return CR_ERR_UNSUPPORTED.  The writer produces
+ * point formats 0-3.
  */
 #ifndef CR_LAZ_H
 #define CR_LAZ_H
@@ -35,15 +38,18 @@ extern "C" {
 
 #define CR_LAZ_MAX_ITEMS 8
 /* LASzip item types (laszip.hpp LASitem::Type) */
-enum { CR_LAZ_ITEM_BYTE = 0, CR_LAZ_ITEM_POINT10 = 6, CR_LAZ_ITEM_GPSTIME11 = 7, CR_LAZ_ITEM_RGB12 = 8 };
+enum {
+    CR_LAZ_ITEM_BYTE = 0, CR_LAZ_ITEM_POINT10 = 6, CR_LAZ_ITEM_GPSTIME11 = 7, CR_LAZ_ITEM_RGB12 = 8,
+    CR_LAZ_ITEM_POINT14 = 10, CR_LAZ_ITEM_RGB14 = 11, CR_LAZ_ITEM_RGBNIR14 = 12, CR_LAZ_ITEM_BYTE14 = 14
+};
 /* LASzip compressors */
-enum { CR_LAZ_POINTWISE = 1, CR_LAZ_POINTWISE_CHUNKED = 2 };
+enum { CR_LAZ_POINTWISE = 1, CR_LAZ_POINTWISE_CHUNKED = 2, CR_LAZ_LAYERED_CHUNKED = 3 };
 #define CR_LAZ_DEFAULT_CHUNK 50000 /* LASzip's default chunk size */
 #define CR_LAZ_VARIABLE_CHUNKS (-1)
 
 typedef struct cr_laz_info {
     cr_las_info las;           /* the public header block, as cr_las_parse_header */
-    int32_t compressor;        /* CR_LAZ_POINTWISE or CR_LAZ_POINTWISE_CHUNKED */
+    int32_t compressor;        /* CR_LAZ_POINTWISE, _POINTWISE_CHUNKED or _LAYERED_CHUNKED */
     int32_t num_items;
     int32_t item_type[CR_LAZ_MAX_ITEMS];
     int32_t item_size[CR_LAZ_MAX_ITEMS];

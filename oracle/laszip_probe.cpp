@@ -17,14 +17,27 @@
 
 namespace {
 
-// Item pointers into one record, in the item order of the LASzip setup.
-void item_pointers(const LASzip& zip, U8* rec, std::vector<U8*>& ptrs) {
-    ptrs.resize(zip.num_items);
-    U32 off = 0;
-    for (U32 i = 0; i < zip.num_items; i++) {
-        ptrs[i] = rec + off;
-        off += zip.items[i].size;
+// Per-item buffers in LASzip's in-memory item layout.  LASzip's raw item
+// readers and writers convert LAS records to and from that layout; for LAS 1.4
+// points the layout's extended_point_type bits (byte 22) must be set, as the
+// LASzip DLL sets them for point formats 6-10.
+struct Items {
+    std::vector<std::vector<U8>> buf;
+    std::vector<U8*> ptr;
+    explicit Items(const LASzip& zip) : buf(zip.num_items, std::vector<U8>(256, 0)), ptr(zip.num_items) {
+        for (U32 i = 0; i < zip.num_items; i++) {
+            ptr[i] = buf[i].data();
+            if (zip.items[i].type == LASitem::POINT14) buf[i][22] = 1;
+        }
     }
+};
+
+bool setup_pair(int point_format, int bytes_per_point, int compressor, uint32_t chunk_size, LASzip& raw,
+                LASzip& packed) {
+    if (!raw.setup((U8)point_format, (U16)bytes_per_point, LASZIP_COMPRESSOR_NONE)) return false;
+    if (!packed.setup((U8)point_format, (U16)bytes_per_point, (U16)compressor)) return false;
+    if (packed.compressor != LASZIP_COMPRESSOR_POINTWISE && !packed.set_chunk_size(chunk_size)) return false;
+    return true;
 }
 
 }  // namespace
@@ -34,9 +47,8 @@ extern "C" {
 // The LASzip VLR payload for a point type / size / compressor / chunk size.
 int lzref_vlr(int point_format, int bytes_per_point, int compressor, uint32_t chunk_size,
               uint8_t* out, int32_t cap) {
-    LASzip zip;
-    if (!zip.setup((U8)point_format, (U16)bytes_per_point, (U16)compressor)) return -1;
-    if (compressor >= LASZIP_COMPRESSOR_POINTWISE_CHUNKED && !zip.set_chunk_size(chunk_size)) return -1;
+    LASzip raw, zip;
+    if (!setup_pair(point_format, bytes_per_point, compressor, chunk_size, raw, zip)) return -1;
     U8* bytes = nullptr;
     I32 num = 0;
     if (!zip.pack(bytes, num) || num > cap) return -1;
@@ -49,21 +61,22 @@ int lzref_vlr(int point_format, int bytes_per_point, int compressor, uint32_t ch
 int64_t lzref_compress(const uint8_t* prefix, int64_t prefix_len, const uint8_t* records, int64_t n,
                        int point_format, int bytes_per_point, int compressor, uint32_t chunk_size,
                        int64_t var_every, uint8_t* out, int64_t cap) {
-    LASzip zip;
-    if (!zip.setup((U8)point_format, (U16)bytes_per_point, (U16)compressor)) return -1;
-    if (compressor >= LASZIP_COMPRESSOR_POINTWISE_CHUNKED && !zip.set_chunk_size(chunk_size)) return -1;
+    LASzip raw, zip;
+    if (!setup_pair(point_format, bytes_per_point, compressor, chunk_size, raw, zip)) return -1;
+    LASreadPoint rr;
+    if (!rr.setup(raw.num_items, raw.items)) return -1;
+    ByteStreamInArrayLE rin(records, n * bytes_per_point);
+    if (!rr.init(&rin)) return -1;
     LASwritePoint w;
     if (!w.setup(zip.num_items, zip.items, &zip)) return -1;
     ByteStreamOutArrayLE os;
     os.putBytes(prefix, (U32)prefix_len);
     if (!w.init(&os)) return -1;
-    std::vector<U8> rec(bytes_per_point);
-    std::vector<U8*> ptrs;
-    item_pointers(zip, rec.data(), ptrs);
+    Items it(zip);
     for (int64_t i = 0; i < n; i++) {
         if (chunk_size == 0xFFFFFFFFu && i > 0 && var_every > 0 && i % var_every == 0) w.chunk();
-        std::memcpy(rec.data(), records + i * bytes_per_point, bytes_per_point);
-        if (!w.write(ptrs.data())) return -1;
+        if (!rr.read(it.ptr.data())) return -1;
+        if (!w.write(it.ptr.data())) return -1;
     }
     if (!w.done()) return -1;
     const int64_t size = os.getSize();
@@ -78,20 +91,30 @@ int64_t lzref_decompress(const uint8_t* file, int64_t size, int64_t points_at, c
                          int32_t vlr_len, int64_t n, int bytes_per_point, uint8_t* records) {
     LASzip zip;
     if (!zip.unpack(vlr, vlr_len)) return -1;
+    U8 point_type = 0;
+    U16 record_length = 0;
+    if (!zip.is_standard(&point_type, &record_length)) return -1;
+    LASzip raw;
+    if (!raw.setup(point_type, record_length, LASZIP_COMPRESSOR_NONE)) return -1;
     LASreadPoint r;
     if (!r.setup(zip.num_items, zip.items, &zip)) return -1;
     ByteStreamInArrayLE is(file, size);
     if (!is.seek(points_at)) return -1;
     if (!r.init(&is)) return -1;
-    std::vector<U8> rec(bytes_per_point);
-    std::vector<U8*> ptrs;
-    item_pointers(zip, rec.data(), ptrs);
-    for (int64_t i = 0; i < n; i++) {
-        if (!r.read(ptrs.data())) return i;
-        std::memcpy(records + i * bytes_per_point, rec.data(), bytes_per_point);
+    LASwritePoint wr;
+    if (!wr.setup(raw.num_items, raw.items)) return -1;
+    ByteStreamOutArrayLE os;
+    if (!wr.init(&os)) return -1;
+    Items it(zip);
+    int64_t i = 0;
+    for (; i < n; i++) {
+        if (!r.read(it.ptr.data())) break;
+        if (!wr.write(it.ptr.data())) return -1;
     }
     r.done();
-    return n;
+    std::memcpy(records, os.getData(), (size_t)os.getSize());
+    (void)bytes_per_point;
+    return i;
 }
 
 }  // extern "C"

@@ -1,5 +1,6 @@
-"""Writes tests/golden/laz/*.laz and tests/golden/laz.json: LAZ files whose
-point data the reference's vendored LASzip compressed (libs/laszip/src, built
+"""Writes tests/golden/laz/*.laz and tests/golden/laz.json: LAZ files (LAS
+point formats 0-3 and the LAS 1.4 formats 6-8) whose point data the
+reference's vendored LASzip compressed (libs/laszip/src, built
 into oracle/_ref/liblaszipref.so by oracle/Makefile from the reference
 checkout), over the deterministic records of tests/helpers.laz_records.  The
 CPU tests decode them with the product's reader, compare the product writer's
@@ -26,6 +27,10 @@ CASES = [
     ("fmt1_extra2", 1, 3000, 2, 2, 1000, 0),
     ("fmt2_12k", 2, 12000, 3, 0, 5000, 0),
     ("fmt3_variable", 3, 5000, 4, 0, -1, 1700),
+    # LAS 1.4, LASzip's layered coder
+    ("fmt6_channels", 6, 4000, 5, 0, 1500, 0),
+    ("fmt7_extra3", 7, 4000, 6, 3, 50000, 0),
+    ("fmt8_variable", 8, 5000, 7, 0, -1, 1800),
 ]
 
 

@@ -212,7 +212,7 @@ def las2_visits(first, num_points, inclusive=True, threads=128, per_thread=80):
     return sorted(out)
 
 
-LAZ_BASE_BYTES = {0: 20, 1: 28, 2: 26, 3: 34}
+LAZ_BASE_BYTES = {0: 20, 1: 28, 2: 26, 3: 34, 6: 30, 7: 36, 8: 38}
 
 
 def _mix(seed: int, i: np.ndarray, lane: int) -> np.ndarray:
@@ -232,6 +232,8 @@ def laz_records(fmt: int, n: int, seed: int, extra: int = 0) -> tuple[np.ndarray
     times rising with repeats and jumps (so LASzip's four time sequences and
     full 64-bit codes are used), 8- and 16-bit and grey colours.  Integer-only
     arithmetic: the same bytes on every host.  -> (records uint8, bpp)."""
+    if fmt >= 6:
+        return _laz_records14(fmt, n, seed, extra)
     bpp = LAZ_BASE_BYTES[fmt] + extra
     i = np.arange(n, dtype=np.uint64)
     h = [_mix(seed, i, lane) for lane in range(16)]
@@ -281,6 +283,74 @@ def laz_records(fmt: int, n: int, seed: int, extra: int = 0) -> tuple[np.ndarray
     return out.reshape(-1), bpp
 
 
+def _laz_records14(fmt: int, n: int, seed: int, extra: int) -> tuple[np.ndarray, int]:
+    """LAS 1.4 point format 6/7/8 records for laz_records: pulses of 1-5
+    returns (a few of up to 15, a few with return 0 or past the count) sharing
+    one GPS time, runs on all four scanner channels with single-point
+    switches, classes past 31, classification flags, negative scan angles."""
+    bpp = LAZ_BASE_BYTES[fmt] + extra
+    i = np.arange(n, dtype=np.uint64)
+    h = [_mix(seed, i, lane) for lane in range(20)]
+    step = lambda hh, r: (hh % np.uint64(2 * r + 1)).astype(np.int64) - r
+    out = np.zeros((n, bpp), np.uint8)
+    xyz = np.stack([5_000_000 + np.cumsum(step(h[0], 900)), -3_000_000 + np.cumsum(step(h[1], 900)),
+                    20_000 + np.cumsum(step(h[2], 150))], axis=1).astype("<i4")
+    out[:, :12] = xyz.view(np.uint8).reshape(n, 12)
+    out[:, 12:14] = ((20000 + np.cumsum(step(h[3], 60))) % 65536).astype("<u2").view(np.uint8).reshape(n, 2)
+    # pulses: a new pulse where the hash says so; return numbers count up inside it
+    start = (h[4] % np.uint64(3)) == 0
+    start[0] = True
+    pulse = np.cumsum(start) - 1
+    first_idx = np.nonzero(start)[0]
+    r = (np.arange(n) - first_idx[pulse]) + 1
+    sizes = np.diff(np.append(first_idx, n))
+    nret = sizes[pulse]
+    big = (_mix(seed, pulse.astype(np.uint64), 30) % np.uint64(50)) == 0
+    nret = np.where(big, np.minimum(nret + 9, 15), nret)
+    odd = (h[5] % np.uint64(97)) == 0
+    r = np.where(odd, (h[6] % np.uint64(16)).astype(np.int64), r)
+    r, nret = np.minimum(r, 15), np.minimum(nret, 15)
+    out[:, 14] = (r | (nret << 4)).astype(np.uint8)
+    run = _mix(seed, i // np.uint64(777), 31) % np.uint64(4)
+    flip = (h[7] % np.uint64(211)) == 0
+    channel = np.where(flip, (run + np.uint64(1) + h[8] % np.uint64(3)) % np.uint64(4), run).astype(np.int64)
+    cflags = np.where((h[9] % np.uint64(50)) == 0, (h[10] % np.uint64(16)).astype(np.int64), 0)
+    sdir = (_mix(seed, i // np.uint64(300), 32) & np.uint64(1)).astype(np.int64)
+    edge = ((h[11] % np.uint64(400)) == 0).astype(np.int64)
+    out[:, 15] = (cflags | (channel << 4) | (sdir << 6) | (edge << 7)).astype(np.uint8)
+    cls = (_mix(seed, i // np.uint64(150), 33) % np.uint64(8)).astype(np.int64)
+    cls = np.choose(cls, [2, 2, 3, 5, 6, 40, 64, 200])
+    out[:, 16] = cls.astype(np.uint8)
+    out[:, 17] = np.where((h[12] % np.uint64(30)) == 0, (h[13] % np.uint64(256)).astype(np.int64), 9) \
+        .astype(np.uint8)
+    angle = (np.cumsum(step(h[14], 3)) % 60001) - 30000
+    angle = np.where((h[15] % np.uint64(4)) == 0, angle, np.roll(angle, 1))
+    out[:, 18:20] = angle.astype("<i2").view(np.uint8).reshape(n, 2)
+    out[:, 20:22] = (_mix(seed, i // np.uint64(4000), 34) % np.uint64(65536)).astype("<u2") \
+        .view(np.uint8).reshape(n, 2)
+    pticks = (300_000 << 20) + np.cumsum((_mix(seed, np.arange(len(first_idx), dtype=np.uint64), 35)
+                                          % np.uint64(4096)).astype(np.int64))
+    ticks = pticks[pulse]
+    jump = (h[16] % np.uint64(1499)) == 0
+    ticks[jump] += ((h[17][jump] % np.uint64(2 << 36)).astype(np.int64) - (1 << 36))
+    out[:, 22:30] = (ticks.astype(np.float64) / float(1 << 20)).astype("<f8").view(np.uint8).reshape(n, 8)
+    off = 30
+    if fmt in (7, 8):
+        rgb = np.stack([(h[18] >> np.uint64(8 * k)) % np.uint64(256) for k in range(4)], axis=1)
+        wide = (h[19] % np.uint64(8)) != 0
+        rgb[wide] *= np.uint64(256)
+        grey = (h[19] % np.uint64(5)) == 0
+        rgb[grey, 1] = rgb[grey, 0]
+        rgb[grey, 2] = rgb[grey, 0]
+        k = 3 if fmt == 7 else 4
+        out[:, off:off + 2 * k] = rgb[:, :k].astype("<u2").view(np.uint8).reshape(n, 2 * k)
+        off += 2 * k
+    if extra:
+        out[:, off:] = ((i[:, None] // np.uint64(5) + np.arange(extra, dtype=np.uint64)[None, :] * np.uint64(7))
+                        % np.uint64(256)).astype(np.uint8)
+    return out.reshape(-1), bpp
+
+
 LAZ_SCALE, LAZ_OFFSET = (0.001, 0.001, 0.001), (0.0, 0.0, 0.0)
 
 
@@ -295,12 +365,14 @@ def laszip_file(records: np.ndarray, n: int, fmt: int, bpp: int, chunk: int = 50
     codec built into oracle/_ref), under the same LAS header and VLR framing
     as compute_rasterizer_gb300.las.laz_bytes."""
     from compute_rasterizer_gb300 import las
+    if fmt >= 6 and compressor == 2:
+        compressor = 3  # LAS 1.4 points take LASzip's layered coder
     lz = O.laszipref()
     vlr = np.zeros(256, np.uint8)
     vn = lz.lzref_vlr(fmt, bpp, compressor, chunk & 0xFFFFFFFF, vlr.ctypes.data, 256)
     assert vn > 0
     bmin, bmax = laz_box(records, n, bpp)
-    head = las._header(n, LAZ_SCALE, LAZ_OFFSET, bmin, bmax, fmt | 128, bpp, (1, 2),
+    head = las._header(n, LAZ_SCALE, LAZ_OFFSET, bmin, bmax, fmt | 128, bpp, (1, 4) if fmt >= 6 else (1, 2),
                        [("laszip encoder", 22204, vlr[:vn].tobytes())])
     pre = np.frombuffer(head, np.uint8).copy()
     rec = np.ascontiguousarray(records, np.uint8)

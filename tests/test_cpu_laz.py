@@ -36,12 +36,15 @@ def test_fixture_decodes_to_its_records(case):
     assert O.fnv(rec) == case["records_fnv"] and bpp == case["bytes_per_point"]
     f = las.LazFile(data)
     assert f.num_points == case["points"] and f.info.las.point_format == case["point_format"]
-    assert f.info.chunk_size == case["chunk_size"] and f.info.compressor == L.LAZ_POINTWISE_CHUNKED
+    layered = case["point_format"] >= 6
+    assert f.info.chunk_size == case["chunk_size"]
+    assert f.info.compressor == (L.LAZ_LAYERED_CHUNKED if layered else L.LAZ_POINTWISE_CHUNKED)
     for threads in (1, 3):
         assert np.array_equal(f.decode(threads=threads), rec)
 
 
-@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+@pytest.mark.parametrize("case", [c for c in CASES if c["point_format"] <= 3],
+                         ids=[c["name"] for c in CASES if c["point_format"] <= 3])
 def test_writer_reproduces_fixture_bytes(case):
     data = (GOLDEN / "laz" / f"{case['name']}.laz").read_bytes()
     rec, bpp = laz_records(case["point_format"], case["points"], case["seed"], case["extra"])
@@ -59,6 +62,36 @@ def test_against_laszip_both_ways(fmt, chunking):
     ref = laszip_file(rec, n, fmt, bpp, chunk, var)
     assert np.array_equal(las.LazFile(ref).decode(threads=4), rec)
     assert product_laz(rec, n, fmt, bpp, chunk, var) == ref
+
+
+@needs_laszip
+@pytest.mark.parametrize("fmt", [6, 7, 8])
+@pytest.mark.parametrize("chunking", [(50000, 0), (611, 0), (-1, 2711), (1, 0)], ids=str)
+def test_layered_las14_against_laszip(fmt, chunking):
+    """LAS 1.4 points through LASzip's layered coder (four scanner channels
+    with switches, pulses sharing a GPS time, classes past 31, extra bytes)."""
+    chunk, var = chunking
+    n = 9001 if chunk != 1 else 200
+    rec, bpp = laz_records(fmt, n, 60 + fmt, extra=2 if fmt == 7 else 0)
+    f = las.LazFile(laszip_file(rec, n, fmt, bpp, chunk, var))
+    assert f.info.compressor == L.LAZ_LAYERED_CHUNKED and f.info.item_version[0] == 3
+    assert np.array_equal(f.decode(threads=4), rec)
+    a, b = n // 7, n // 7 + n // 2
+    assert np.array_equal(f.decode(a, b - a, threads=2), rec[a * bpp:b * bpp])
+
+
+@needs_laszip
+def test_layered_random_records():
+    """Every byte of format-8 records random but the GPS time: every return,
+    flag and channel combination, empty and full layers side by side."""
+    rng = np.random.default_rng(23)
+    n, fmt, bpp = 5000, 8, 40
+    rec = rng.integers(0, 256, n * bpp, dtype=np.uint8)
+    t = rec.reshape(n, bpp)
+    t[:, 22:30] = rng.normal(4e5, 10.0, n).astype("<f8").view(np.uint8).reshape(n, 8)
+    t[: n // 2, 36:38] = 7  # the NIR layer's first chunk stays empty
+    f = las.LazFile(laszip_file(rec, n, fmt, bpp, 2500))
+    assert np.array_equal(f.decode(), rec)
 
 
 @needs_laszip
@@ -140,7 +173,9 @@ def test_error_statuses():
     assert status(las_file) == L.INVALID_ARG  # no LASzip VLR
     vlr_at = struct.unpack_from("<H", good, 94)[0] + 54
     bad = bytearray(good)
-    struct.pack_into("<H", bad, vlr_at, 3)  # layered compressor
+    struct.pack_into("<H", bad, vlr_at, 3)  # the layered compressor over point-wise items
+    assert status(bad) == L.INVALID_ARG
+    struct.pack_into("<H", bad, vlr_at, 4)  # no such compressor
     assert status(bad) == L.UNSUPPORTED
     bad = bytearray(good)
     struct.pack_into("<H", bad, vlr_at + 38, 1)  # POINT10 version 1
@@ -151,6 +186,11 @@ def test_error_statuses():
     bad[mid:mid + 64] = bytes(64)  # a chunk's coder bytes zeroed
     assert status(bad) == L.CORRUPT
     assert lib.cr_laz_decode(None, 0, 1, None, 1) == L.INVALID_ARG
+    bad = bytearray(good)
+    struct.pack_into("<H", bad, vlr_at + 34, L.LAZ_ITEM_POINT14)  # a LAS 1.4 item in a point-wise stream
+    struct.pack_into("<H", bad, vlr_at + 36, 30)
+    struct.pack_into("<H", bad, vlr_at + 38, 3)
+    assert status(bad) == L.INVALID_ARG
     vlen = C.c_int64()
     assert lib.cr_laz_vlr(6, 30, 50000, None, 0, C.byref(vlen)) == L.UNSUPPORTED
     assert lib.cr_laz_vlr(2, 20, 50000, None, 0, C.byref(vlen)) == L.INVALID_ARG

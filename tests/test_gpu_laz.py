@@ -1,7 +1,8 @@
 """LAZ ingest on the GPU (include/cr_laz.h): the committed LAZ files whose
-point data LASzip wrote load into clouds whose batch records and word streams
-equal the oracle's loadLas encoding of the same records (colour 0 for point
-formats without RGB, as loadLaz reads LASzip's zeroed rgb), render as the
+point data LASzip wrote (point formats 0-3 and the LAS 1.4 formats 6-8) load
+into clouds whose batch records and word streams equal the oracle's loadLas
+encoding of the same records (colour 0 for point formats without RGB, as
+loadLaz reads LASzip's zeroed rgb), render as the
 oracle renders them, load beside LAS files in one cloud, and a multi-window
 file written by the product's writer equals the LAS path of its records."""
 import json
@@ -33,7 +34,7 @@ def oracle_layout(rec, n, bpp, fmt, bmin, point=0, file_index=0):
                            sparse_offset=point + t0, file_index=file_index)
         parts.append(out)
     lay = [np.concatenate([p[k] for p in parts]) for k in range(5)]
-    if fmt in (0, 1):
+    if fmt in (0, 1, 6):
         lay[4][:] = 0
     return lay
 

@@ -15,8 +15,10 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -1783,44 +1785,125 @@ cr_status cr_cloud_load_laz(cr_ctx* ctx, cr_cloud* cloud, const cr_laz* laz, int
 
     const int64_t bpp = laz->layout.bpp, task = CR_MAX_POINTS_PER_LOAD;
     const int nthreads = resolve_threads(threads, 1 << 20);
-    // windows of whole load tasks holding about four chunks per thread
-    const int64_t chunk = laz->chunk_points > 0 ? laz->chunk_points : CR_LAZ_DEFAULT_CHUNK;
-    int64_t window = std::max<int64_t>(1, (4 * nthreads * chunk + task - 1) / task) * task;
+    // windows of whole load tasks holding about four chunks per thread, and at
+    // least the largest chunk (so a chunk touches at most two windows)
+    int64_t max_chunk = laz->chunk_points > 0 ? laz->chunk_points : CR_LAZ_DEFAULT_CHUNK;
+    for (size_t c = 0; c + 1 < laz->chunk_first.size(); c++)
+        max_chunk = std::max(max_chunk, laz->chunk_first[c + 1] - laz->chunk_first[c]);
+    int64_t window = std::max<int64_t>(1, (4 * nthreads * max_chunk + task - 1) / task) * task;
+    window = std::max(window, (max_chunk + task - 1) / task * task);
     window = std::min(window, (n + task - 1) / task * task);
-    uint8_t* host[2] = {nullptr, nullptr};
+    const int64_t nwin = (n + window - 1) / window;
+    const bool pipelined = !laz->sequential && laz->info.compressor != CR_LAZ_POINTWISE && nwin > 1;
+    const int R = pipelined ? 3 : 2;  // host window slots
+    uint8_t* host[3] = {nullptr, nullptr, nullptr};
     uint8_t* staging = nullptr;
-    cudaEvent_t copied[2] = {nullptr, nullptr};
+    cudaEvent_t copied[3] = {nullptr, nullptr, nullptr};
     cudaStream_t st = (cudaStream_t)stream;
-    cudaError_t e = cudaHostAlloc(&host[0], (size_t)(window * bpp), cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaHostAlloc(&host[1], (size_t)(window * bpp), cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaMalloc(&staging, (size_t)(window * bpp));
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied[0], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied[1], cudaEventDisableTiming);
+    cudaError_t e = cudaMalloc(&staging, (size_t)(window * bpp));
+    for (int r = 0; r < R && e == cudaSuccess; r++) {
+        e = cudaHostAlloc(&host[r], (size_t)(window * bpp), cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied[r], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) s = e == cudaErrorMemoryAllocation ? CR_ERR_OUT_OF_MEMORY : CR_ERR_CUDA;
     int64_t b = batch_offset;
-    for (int64_t w0 = 0, wi = 0; s == CR_OK && w0 < n; w0 += window, wi++) {
-        const int64_t cnt = std::min(window, n - w0);
-        uint8_t* buf = host[wi & 1];
-        // the copy that last read this buffer has finished
-        if (wi >= 2 && cudaEventSynchronize(copied[wi & 1]) != cudaSuccess) {
-            s = CR_ERR_CUDA;
-            break;
-        }
-        s = decode_range(laz, w0, cnt, buf, nthreads);
-        if (s != CR_OK) break;
-        if (cudaMemcpyAsync(staging, buf, (size_t)(cnt * bpp), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaEventRecord(copied[wi & 1], st) != cudaSuccess) {
-            s = CR_ERR_CUDA;
-            break;
-        }
-        for (int64_t t0 = 0; t0 < cnt && s == CR_OK; t0 += task) {
+    // window wi's records in host[slot]: copied to the device and encoded task by task
+    auto ship = [&](int64_t wi, int slot) -> cr_status {
+        const int64_t w0 = wi * window, cnt = std::min(window, n - w0);
+        if (cudaMemcpyAsync(staging, host[slot], (size_t)(cnt * bpp), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaEventRecord(copied[slot], st) != cudaSuccess)
+            return CR_ERR_CUDA;
+        for (int64_t t0 = 0; t0 < cnt; t0 += task) {
             const int64_t tc = std::min(task, cnt - t0);
             const int64_t p = point_offset + w0 + t0;
-            s = cr::encode_records_device(staging + t0 * bpp, tc, (int32_t)bpp, laz->layout.rgb_offset,
-                                          laz->info.las.scale, laz->info.las.offset, laz->info.las.min, p,
-                                          file_index, batches + b, lo + p, md + p, hi + p, rgba + p, st);
+            const cr_status es = cr::encode_records_device(
+                staging + t0 * bpp, tc, (int32_t)bpp, laz->layout.rgb_offset, laz->info.las.scale,
+                laz->info.las.offset, laz->info.las.min, p, file_index, batches + b, lo + p, md + p, hi + p,
+                rgba + p, st);
+            if (es != CR_OK) return es;
             b += cr_num_batches(tc);
         }
+        return CR_OK;
+    };
+    if (s == CR_OK && !pipelined) {
+        // one window at a time, decoded while the previous one is copied and encoded
+        for (int64_t wi = 0; s == CR_OK && wi < nwin; wi++) {
+            const int slot = (int)(wi % R);
+            if (wi >= R && cudaEventSynchronize(copied[slot]) != cudaSuccess) {
+                s = CR_ERR_CUDA;
+                break;
+            }
+            s = decode_range(laz, wi * window, std::min(window, n - wi * window), host[slot], nthreads);
+            if (s == CR_OK) s = ship(wi, slot);
+        }
+    } else if (s == CR_OK) {
+        // Every thread decodes chunks in file order into the slot of their
+        // window (a chunk across a window border into both); this thread ships
+        // each window once all its points are decoded, and hands the slot to
+        // window wi + R once the copy has read it.
+        const auto& cf = laz->chunk_first;
+        const int64_t nchunks = (int64_t)cf.size() - 1;
+        std::mutex mu;
+        std::condition_variable cv;
+        std::vector<int64_t> owner(R), left(nwin);
+        for (int r = 0; r < R; r++) owner[r] = r < nwin ? r : -1;
+        for (int64_t wi = 0; wi < nwin; wi++) left[wi] = std::min(window, n - wi * window);
+        bool failed = false;
+        std::atomic<int64_t> next(0);
+        const uint8_t* file_end = laz->file + laz->size;
+        auto worker = [&]() {
+            PointCodec codec(laz->layout, true);
+            std::vector<uint8_t> tmp;
+            for (int64_t c = next++; c < nchunks; c = next++) {
+                const int64_t clo = cf[c], chi = std::min(cf[c + 1], n);
+                if (clo >= chi) continue;
+                const int64_t wa = clo / window, wb = (chi - 1) / window;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&] { return failed || (owner[wa % R] == wa && owner[wb % R] == wb); });
+                    if (failed) return;
+                }
+                const int64_t count = cf[c + 1] - clo;
+                uint8_t* dst;
+                if (wa == wb) {
+                    dst = host[wa % R] + (clo - wa * window) * bpp;
+                } else {
+                    tmp.resize((size_t)((chi - clo) * bpp));
+                    dst = tmp.data();
+                }
+                const uint8_t* end = nullptr;
+                const bool ok = codec.decode_chunk(laz->file + laz->chunk_start[c], file_end, count, 0, chi - clo,
+                                                   chi - clo, dst, &end) &&
+                                (chi - clo < count || end == laz->file + laz->chunk_start[c + 1]);
+                if (ok && wa != wb) {  // split across the border
+                    const int64_t border = wb * window;
+                    std::memcpy(host[wa % R] + (clo - wa * window) * bpp, tmp.data(), (size_t)((border - clo) * bpp));
+                    std::memcpy(host[wb % R], tmp.data() + (border - clo) * bpp, (size_t)((chi - border) * bpp));
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                if (!ok) failed = true;
+                left[wa] -= std::min(chi, (wa + 1) * window) - clo;
+                if (wb != wa) left[wb] -= chi - wb * window;
+                cv.notify_all();
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; t++) pool.emplace_back(worker);
+        for (int64_t wi = 0; wi < nwin && s == CR_OK; wi++) {
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return failed || left[wi] == 0; });
+                if (failed) s = CR_ERR_CORRUPT;
+            }
+            const int slot = (int)(wi % R);
+            if (s == CR_OK) s = ship(wi, slot);
+            if (s == CR_OK && cudaEventSynchronize(copied[slot]) != cudaSuccess) s = CR_ERR_CUDA;
+            std::lock_guard<std::mutex> lk(mu);
+            if (s != CR_OK) failed = true;
+            else if (wi + R < nwin) owner[slot] = wi + R;
+            cv.notify_all();
+        }
+        for (auto& th : pool) th.join();
     }
     if (cudaStreamSynchronize(st) != cudaSuccess && s == CR_OK) s = CR_ERR_CUDA;
     for (cudaEvent_t ev : copied)

@@ -93,9 +93,10 @@ def test_laz_beside_las_files(ctx, tmp_path):
 
 
 def test_multi_window_file_equals_las_path(ctx, tmp_path):
-    """3.1M points in load tasks of 1,024,000, decoded in one-task windows on
-    one thread (four windows through the double-buffered upload) and in one
-    window on all threads: both equal the LAS path of the same records."""
+    """3.1M points in load tasks of 1,024,000, decoded in windows of whole
+    tasks through the pipelined upload (chunks of 50,000 and of 700,000
+    points, some across window borders) and in one window on all threads:
+    every load equals the LAS path of the same records."""
     n, fmt = 3_100_000, 2
     p = synth.synth_params(L.SYNTH_TERRAIN, 800.0, 12)
     rec, hdr = synth.las_records_host(p, n)
@@ -104,10 +105,15 @@ def test_multi_window_file_equals_las_path(ctx, tmp_path):
     ref, _ = las.load_files(ctx, [ls])
     ctx.sync()
     want = [ref.read(0)] + [ref.read(s) for s in STREAMS]
-    for threads in (1, 0):
-        cloud, _ = las.load_files(ctx, [lz], threads=threads)
+    lz2 = las.write_laz(tmp_path / "big_var.laz", rec, n, hdr.scale, hdr.offset, hdr.min, hdr.max,
+                        chunk_size=L.LAZ_VARIABLE_CHUNKS, var_chunk=700_000)
+    # one-task windows on one thread and on two (pipelined, chunks across
+    # window borders), 3-task windows of 700,000-point chunks on one thread,
+    # one window on all threads
+    for path, threads in ((lz, 1), (lz, 2), (lz2, 1), (lz, 0)):
+        cloud, _ = las.load_files(ctx, [path], threads=threads)
         ctx.sync()
-        assert np.array_equal(cloud.read(0).view(np.uint8), want[0].view(np.uint8))
+        assert np.array_equal(cloud.read(0).view(np.uint8), want[0].view(np.uint8)), (path, threads)
         for which, w in zip(STREAMS, want[1:]):
-            assert np.array_equal(cloud.read(which), w), (threads, which)
+            assert np.array_equal(cloud.read(which), w), (path, threads, which)
         cloud.close()

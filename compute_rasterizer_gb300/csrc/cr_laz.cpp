@@ -1445,12 +1445,15 @@ class PointCodec {
         }
         size_t li = 0;
         const uint8_t* at = q;
+        bool overrun = false;
         auto layer = [&](Decoder& d, bool always) -> bool {  // one layer's bytes; false: empty
             const uint32_t n = sizes[li++];
+            const bool fits = (int64_t)n <= file_end - at;
             d.p = at;
-            d.end = at + n;
-            d.bad = (int64_t)n > file_end - at;
-            at += n;
+            d.end = fits ? at + n : file_end;  // never past the file
+            d.bad = !fits;
+            overrun |= !fits;
+            at = fits ? at + n : file_end;
             if (n == 0 && !always) return false;
             d.start();
             return true;
@@ -1467,7 +1470,7 @@ class PointCodec {
                 for (int k = 0; k < it.size; k++) bytes14_->changed[k] = layer(bytes14_->d[k], false);
             }
         }
-        if (at > file_end) return false;
+        if (overrun) return false;
         // POINT14 comes first and hands its scanner channel to the others
         uint32_t shared = 0;
         size_t off = 0;

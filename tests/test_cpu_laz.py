@@ -194,3 +194,36 @@ def test_error_statuses():
     vlen = C.c_int64()
     assert lib.cr_laz_vlr(6, 30, 50000, None, 0, C.byref(vlen)) == L.UNSUPPORTED
     assert lib.cr_laz_vlr(2, 20, 50000, None, 0, C.byref(vlen)) == L.INVALID_ARG
+
+
+@pytest.mark.parametrize("case", ["fmt2_12k", "fmt7_extra3", "fmt8_variable"])
+def test_corrupted_files_fail_cleanly(case):
+    """Random byte flips and cuts anywhere in a file (header, VLR, chunk
+    table, layer sizes, coder bytes): every open and decode returns a status
+    or some records, never reads outside the file (the decoders and layer
+    extents are clamped to it)."""
+    lib = L.load()
+    data = (GOLDEN / "laz" / f"{case}.laz").read_bytes()
+    rng = np.random.default_rng(99)
+    seen = set()
+    for it in range(120):
+        buf = bytearray(data)
+        if it % 3 == 0:
+            buf = buf[: int(rng.integers(1, len(buf)))]
+        else:
+            for _ in range(int(rng.integers(1, 8))):
+                k = int(rng.integers(0, len(buf)))
+                buf[k] = int(rng.integers(0, 256))
+        arr = np.frombuffer(bytes(buf), np.uint8)
+        h, info = C.c_void_p(), L.LazInfo()
+        st = lib.cr_laz_open(arr.ctypes.data, arr.size, C.byref(h), C.byref(info))
+        if st == L.OK:
+            n = int(info.las.num_points)
+            bpp = int(info.las.bytes_per_point)
+            if 0 < n <= 200_000 and 0 < bpp <= 512:
+                out = np.zeros(n * bpp, np.uint8)
+                st = lib.cr_laz_decode(h, 0, n, out.ctypes.data, 2)
+            lib.cr_laz_close(h)
+        assert st in (L.OK, L.INVALID_ARG, L.UNSUPPORTED, L.CORRUPT)
+        seen.add(st)
+    assert L.CORRUPT in seen or L.INVALID_ARG in seen

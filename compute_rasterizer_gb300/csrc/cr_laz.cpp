@@ -1065,10 +1065,12 @@ struct P14Context {
 };
 
 struct Point14Layered {
+    bool v4;  // version 4 hands its channel to the other items on every point
     std::unique_ptr<P14Context> ctx[4];
     uint32_t cur = 0, gen = 0;
     Decoder d[kP14Layers];
     bool changed[kP14Layers];
+    explicit Point14Layered(bool version4) : v4(version4) {}
 
     P14Context& context(uint32_t c) {
         if (!ctx[c]) ctx[c].reset(new P14Context());
@@ -1099,6 +1101,7 @@ struct Point14Layered {
             c = &nc;
             c->last.channel = sc;
         }
+        if (v4) shared = cur;
         Point14& L = c->last;
         const bool source_change = (cv & (1u << 5)) != 0;
         const uint32_t gps_change = (cv >> 4) & 1u;
@@ -1195,12 +1198,12 @@ struct RgbCtx {
 };
 
 struct Rgb14Layered {
-    bool nir;
+    bool nir, v4;  // version 4 also switches to a used context's own last values
     std::unique_ptr<RgbCtx> ctx[4];
     uint32_t cur = 0;
     Decoder d[2];  // RGB, NIR
     bool changed[2];
-    explicit Rgb14Layered(bool with_nir) : nir(with_nir) {}
+    Rgb14Layered(bool with_nir, bool version4) : nir(with_nir), v4(version4) {}
 
     RgbCtx& context(uint32_t c) {
         if (!ctx[c]) ctx[c].reset(new RgbCtx(nir));
@@ -1221,6 +1224,8 @@ struct Rgb14Layered {
             RgbCtx& nc = context(cur);
             if (!nc.used) {
                 nc.init(last, nir);
+                last = nc.last;
+            } else if (v4) {
                 last = nc.last;
             }
         }
@@ -1263,11 +1268,12 @@ struct BytesCtx {
 
 struct Bytes14Layered {
     uint32_t count;
+    bool v4;
     std::unique_ptr<BytesCtx> ctx[4];
     uint32_t cur = 0;
     std::vector<Decoder> d;
     std::vector<uint8_t> changed;
-    explicit Bytes14Layered(uint32_t n) : count(n), d(n), changed(n) {}
+    Bytes14Layered(uint32_t n, bool version4) : count(n), v4(version4), d(n), changed(n) {}
 
     BytesCtx& context(uint32_t c) {
         if (!ctx[c]) ctx[c].reset(new BytesCtx(count));
@@ -1291,6 +1297,8 @@ struct Bytes14Layered {
             BytesCtx& nc = context(cur);
             if (!nc.used) {
                 init_context(nc, last);
+                last = nc.last.data();
+            } else if (v4) {
                 last = nc.last.data();
             }
         }
@@ -1347,10 +1355,12 @@ class PointCodec {
                 case CR_LAZ_ITEM_POINT10: p10_.reset(new Point10(decoder)); break;
                 case CR_LAZ_ITEM_GPSTIME11: gps_.reset(new GpsTime11(decoder)); break;
                 case CR_LAZ_ITEM_RGB12: rgb_.reset(new Rgb12(decoder)); break;
-                case CR_LAZ_ITEM_POINT14: p14_.reset(new Point14Layered()); break;
-                case CR_LAZ_ITEM_RGB14: rgb14_.reset(new Rgb14Layered(false)); break;
-                case CR_LAZ_ITEM_RGBNIR14: rgb14_.reset(new Rgb14Layered(true)); break;
-                case CR_LAZ_ITEM_BYTE14: bytes14_.reset(new Bytes14Layered((uint32_t)it.size)); break;
+                case CR_LAZ_ITEM_POINT14: p14_.reset(new Point14Layered(it.version == 4)); break;
+                case CR_LAZ_ITEM_RGB14: rgb14_.reset(new Rgb14Layered(false, it.version == 4)); break;
+                case CR_LAZ_ITEM_RGBNIR14: rgb14_.reset(new Rgb14Layered(true, it.version == 4)); break;
+                case CR_LAZ_ITEM_BYTE14:
+                    bytes14_.reset(new Bytes14Layered((uint32_t)it.size, it.version == 4));
+                    break;
                 default: bytes_.reset(new Bytes((uint32_t)it.size, decoder)); break;
             }
         }
@@ -1700,7 +1710,7 @@ cr_status cr_laz_open(const void* file, int64_t size, cr_laz** out, cr_laz_info*
                         (it.type == CR_LAZ_ITEM_RGB14 && it.size == 6) ||
                         (it.type == CR_LAZ_ITEM_RGBNIR14 && it.size == 8) ||
                         (it.type == CR_LAZ_ITEM_BYTE14 && it.size >= 1);
-        if (!(v2 && it.version == 2) && !(v3 && it.version == 3)) st = CR_ERR_UNSUPPORTED;
+        if (!(v2 && it.version == 2) && !(v3 && (it.version == 3 || it.version == 4))) st = CR_ERR_UNSUPPORTED;
         else if (seen[it.type]) st = CR_ERR_INVALID_ARG;
         else seen[it.type] = true;
         if (it.type == CR_LAZ_ITEM_RGB12 || it.type == CR_LAZ_ITEM_RGB14 || it.type == CR_LAZ_ITEM_RGBNIR14)

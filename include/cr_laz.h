@@ -23,9 +23,9 @@
  * RGB12 and BYTE (LAS point formats 0-3 plus extra bytes); and the layered
  * coder of LAS 1.4 (compressor 3) with version-3 items POINT14, RGB14,
  * RGBNIR14 and BYTE14 (point formats 6, 7 and 8 plus extra bytes), as
- * LASzip 3.4 writes them.  Version-1 and version-4 items and wave packets
- * (formats 4, 5, 9, 10) return CR_ERR_UNSUPPORTED.  The writer produces
- * point formats 0-3.
+ * LASzip 3.4 writes them, and their version-4 revision.  Version-1 items and
+ * wave packets (formats 4, 5, 9, 10) return CR_ERR_UNSUPPORTED.  The writer
+ * produces point formats 0-3.
  */
 #ifndef CR_LAZ_H
 #define CR_LAZ_H

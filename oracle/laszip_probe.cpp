@@ -32,11 +32,17 @@ struct Items {
     }
 };
 
-bool setup_pair(int point_format, int bytes_per_point, int compressor, uint32_t chunk_size, LASzip& raw,
-                LASzip& packed) {
+// item_version 4 selects LASzip's version-4 LAS 1.4 items (its fix of the
+// version-3 context hand-over), which the library writes when an item asks
+// for it; 0 keeps LASzip's default.
+bool setup_pair(int point_format, int bytes_per_point, int compressor, uint32_t chunk_size, int item_version,
+                LASzip& raw, LASzip& packed) {
     if (!raw.setup((U8)point_format, (U16)bytes_per_point, LASZIP_COMPRESSOR_NONE)) return false;
     if (!packed.setup((U8)point_format, (U16)bytes_per_point, (U16)compressor)) return false;
     if (packed.compressor != LASZIP_COMPRESSOR_POINTWISE && !packed.set_chunk_size(chunk_size)) return false;
+    if (item_version == 4)
+        for (U32 i = 0; i < packed.num_items; i++)
+            if (packed.items[i].version == 3) packed.items[i].version = 4;
     return true;
 }
 
@@ -46,9 +52,9 @@ extern "C" {
 
 // The LASzip VLR payload for a point type / size / compressor / chunk size.
 int lzref_vlr(int point_format, int bytes_per_point, int compressor, uint32_t chunk_size,
-              uint8_t* out, int32_t cap) {
+              int item_version, uint8_t* out, int32_t cap) {
     LASzip raw, zip;
-    if (!setup_pair(point_format, bytes_per_point, compressor, chunk_size, raw, zip)) return -1;
+    if (!setup_pair(point_format, bytes_per_point, compressor, chunk_size, item_version, raw, zip)) return -1;
     U8* bytes = nullptr;
     I32 num = 0;
     if (!zip.pack(bytes, num) || num > cap) return -1;
@@ -60,9 +66,9 @@ int lzref_vlr(int point_format, int bytes_per_point, int compressor, uint32_t ch
 // chunk size of 0xFFFFFFFF a chunk is closed after every `var_every` points.
 int64_t lzref_compress(const uint8_t* prefix, int64_t prefix_len, const uint8_t* records, int64_t n,
                        int point_format, int bytes_per_point, int compressor, uint32_t chunk_size,
-                       int64_t var_every, uint8_t* out, int64_t cap) {
+                       int item_version, int64_t var_every, uint8_t* out, int64_t cap) {
     LASzip raw, zip;
-    if (!setup_pair(point_format, bytes_per_point, compressor, chunk_size, raw, zip)) return -1;
+    if (!setup_pair(point_format, bytes_per_point, compressor, chunk_size, item_version, raw, zip)) return -1;
     LASreadPoint rr;
     if (!rr.setup(raw.num_items, raw.items)) return -1;
     ByteStreamInArrayLE rin(records, n * bytes_per_point);

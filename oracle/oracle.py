@@ -131,9 +131,9 @@ def laszipref() -> C.CDLL:
     """The LASzip probe built from the reference's vendored LASzip (oracle/_ref)."""
     g = C.CDLL(str(LAZREF))
     P, I, I64, U32 = C.c_void_p, C.c_int, C.c_int64, C.c_uint32
-    g.lzref_vlr.argtypes = [I, I, I, U32, P, C.c_int32]
+    g.lzref_vlr.argtypes = [I, I, I, U32, I, P, C.c_int32]
     g.lzref_vlr.restype = C.c_int
-    g.lzref_compress.argtypes = [P, I64, P, I64, I, I, I, U32, I64, P, I64]
+    g.lzref_compress.argtypes = [P, I64, P, I64, I, I, I, U32, I, I64, P, I64]
     g.lzref_compress.restype = I64
     g.lzref_decompress.argtypes = [P, I64, I64, P, C.c_int32, I64, I, P]
     g.lzref_decompress.restype = I64

@@ -360,7 +360,7 @@ def laz_box(records: np.ndarray, n: int, bpp: int):
 
 
 def laszip_file(records: np.ndarray, n: int, fmt: int, bpp: int, chunk: int = 50000, var_every: int = 0,
-                compressor: int = 2) -> bytes:
+                compressor: int = 2, item_version: int = 0) -> bytes:
     """A LAZ file whose point data LASzip itself wrote (the reference's vendored
     codec built into oracle/_ref), under the same LAS header and VLR framing
     as compute_rasterizer_gb300.las.laz_bytes."""
@@ -369,7 +369,7 @@ def laszip_file(records: np.ndarray, n: int, fmt: int, bpp: int, chunk: int = 50
         compressor = 3  # LAS 1.4 points take LASzip's layered coder
     lz = O.laszipref()
     vlr = np.zeros(256, np.uint8)
-    vn = lz.lzref_vlr(fmt, bpp, compressor, chunk & 0xFFFFFFFF, vlr.ctypes.data, 256)
+    vn = lz.lzref_vlr(fmt, bpp, compressor, chunk & 0xFFFFFFFF, item_version, vlr.ctypes.data, 256)
     assert vn > 0
     bmin, bmax = laz_box(records, n, bpp)
     head = las._header(n, LAZ_SCALE, LAZ_OFFSET, bmin, bmax, fmt | 128, bpp, (1, 4) if fmt >= 6 else (1, 2),
@@ -378,6 +378,6 @@ def laszip_file(records: np.ndarray, n: int, fmt: int, bpp: int, chunk: int = 50
     rec = np.ascontiguousarray(records, np.uint8)
     out = np.zeros(n * bpp * 2 + 65536, np.uint8)
     size = lz.lzref_compress(pre.ctypes.data, pre.size, rec.ctypes.data, n, fmt, bpp, compressor,
-                             chunk & 0xFFFFFFFF, var_every, out.ctypes.data, out.size)
+                             chunk & 0xFFFFFFFF, item_version, var_every, out.ctypes.data, out.size)
     assert size > 0, size
     return out[:size].tobytes()

@@ -65,16 +65,18 @@ def test_against_laszip_both_ways(fmt, chunking):
 
 
 @needs_laszip
+@pytest.mark.parametrize("version", [3, 4])
 @pytest.mark.parametrize("fmt", [6, 7, 8])
 @pytest.mark.parametrize("chunking", [(50000, 0), (611, 0), (-1, 2711), (1, 0)], ids=str)
-def test_layered_las14_against_laszip(fmt, chunking):
-    """LAS 1.4 points through LASzip's layered coder (four scanner channels
-    with switches, pulses sharing a GPS time, classes past 31, extra bytes)."""
+def test_layered_las14_against_laszip(fmt, chunking, version):
+    """LAS 1.4 points through LASzip's layered coder, item versions 3 (its
+    default) and 4 (its fix of the context hand-over): four scanner channels
+    with switches, pulses sharing a GPS time, classes past 31, extra bytes."""
     chunk, var = chunking
     n = 9001 if chunk != 1 else 200
     rec, bpp = laz_records(fmt, n, 60 + fmt, extra=2 if fmt == 7 else 0)
-    f = las.LazFile(laszip_file(rec, n, fmt, bpp, chunk, var))
-    assert f.info.compressor == L.LAZ_LAYERED_CHUNKED and f.info.item_version[0] == 3
+    f = las.LazFile(laszip_file(rec, n, fmt, bpp, chunk, var, item_version=version))
+    assert f.info.compressor == L.LAZ_LAYERED_CHUNKED and f.info.item_version[0] == version
     assert np.array_equal(f.decode(threads=4), rec)
     a, b = n // 7, n // 7 + n // 2
     assert np.array_equal(f.decode(a, b - a, threads=2), rec[a * bpp:b * bpp])

@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--cpu-table", action="store_true",
                     help="time the oracle per workload on this host's cores and exit")
     ap.add_argument("--serving", default="quick", choices=["quick", "full", "off"])
-    ap.add_argument("--extras", default="payloads,multiview,configs,serving,ingest",
+    ap.add_argument("--extras", default="payloads,multiview,configs,serving,ingest,potree",
                     help="comma list of extra workloads after the headline frame")
     return ap.parse_args()
 
@@ -409,7 +409,8 @@ def main():
         runs = [("payloads", lambda: extras(ctx, cloud, cv, fb, sh, n, args)),
                 ("multiview", lambda: {"multiview_64": multiview_64(ctx, sh, args.steps, payload)}),
                 ("configs", lambda: small_configs(ctx, sh, args, payload)),
-                ("ingest", lambda: {"ingest": ingest(ctx, sh)})]
+                ("ingest", lambda: {"ingest": ingest(ctx, sh)}),
+                ("potree", lambda: {"potree_loop_nodes": potree_nodes(ctx, sh, args.steps)})]
         if args.serving != "off":
             runs.append(("serving", lambda: {"serving": serving(ctx, sh, args, payload)}))
         for name, fn in runs:
@@ -550,6 +551,86 @@ def ingest(ctx, sh, points=50_000_000):
             "laz_equals_las_cloud": bool(same),
             "what": "cr_cloud_load_las / cr_cloud_load_laz wall clock from host memory; decode-only "
                     "cr_laz_decode on all threads and on one (5M points)"}
+
+
+def potree_nodes(ctx, sh, steps, points=10_000_000):
+    """loop_nodes ("render Potree nodes", compute_loop_nodes) on a Potree 2.0
+    dataset: a Morton-sorted terrain of `points` records (generated and sorted
+    on the GPU) written by potree.write_octree (hashed 1/8 samples in inner
+    nodes, leaves of at most 20,000 points, hierarchy chunks of 2 levels),
+    opened and loaded through the C ABI (metadata.json, hierarchy.bin,
+    octree.bin encoded one batch record per node) and rendered at 1920x1080
+    from the zoom-to-cloud pose with the method's defaults (level-4 cut, node
+    loop, float uniforms, tiled resolve); CUDA events over the frames."""
+    import ctypes as C
+    import shutil
+    import tempfile
+    import time
+
+    import torch
+
+    import compute_rasterizer_gb300 as cr
+    from compute_rasterizer_gb300 import _lib as L
+    from compute_rasterizer_gb300 import potree, synth
+    lib = L.load()
+    n, bpp = points, L.LAS_FORMAT2_BYTES
+    p = synth.synth_params(L.SYNTH_TERRAIN, 1500.0, 31)
+    hdr = L.LasHeader()
+    rec_d = torch.empty(n * bpp, dtype=torch.uint8, device="cuda")
+    ctx.check(lib.cr_synth_points_device(ctx.handle, C.byref(p), n, rec_d.data_ptr(), C.byref(hdr), sh), "gen")
+    ctx.check(lib.cr_morton_sort_device(ctx.handle, rec_d.data_ptr(), n, bpp, C.byref(hdr), sh), "sort")
+    ctx.sync(sh)
+    rec = rec_d.cpu().numpy()
+    del rec_d
+    d = tempfile.mkdtemp(prefix="cr_potree_")
+    try:
+        t0 = time.perf_counter()
+        nodes = potree.write_octree(d, rec, n, hdr.scale[:], hdr.offset[:], hdr.min[:], hdr.max[:],
+                                    max_leaf=20000, chunk_levels=2)
+        write_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o = potree.open_octree(d)
+        cloud = o.load(ctx, stream=sh)
+        ctx.sync(sh)
+        load_s = time.perf_counter() - t0
+        extent = np.array(hdr.max[:]) - np.array(hdr.min[:])
+        yaw, pitch, radius, target = synth.zoom_to_cloud(np.zeros(3), extent)
+        W, H = 1920, 1080
+        view = synth.orbit_view(yaw, pitch, radius, target)
+        cv = cr.make_view(view, synth.perspective(60.0, W / H, 0.1, 200000.0), W, H)
+        params = cr.default_params(L.METHOD_LOOP_NODES)
+        fb = ctx.framebuffer(W, H)
+        fb.clear(stream=sh)
+        stream = torch.cuda.ExternalStream(sh)
+        for _ in range(3):
+            ctx.render(cloud, cv, params, fb, sh)
+        ctx.sync(sh)
+        k = max(5, min(steps, 50))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            ctx.render(cloud, cv, params, fb, sh)
+        e1.record(stream)
+        ctx.sync(sh)
+        ms = e0.elapsed_time(e1) / k
+        st = ctx.frame_stats(cloud, params)
+        peak, _ = measured_peaks()
+        out = {"points": n, "nodes": len(nodes), "levels": int(max(nd["level"] for nd in nodes)) + 1,
+               "max_node_points": int(max(nd["num_points"] for nd in nodes)),
+               "ms_per_frame": round(ms, 4), "gpoints_per_s": round(n / ms / 1e6, 2),
+               "points_per_level": list(st.points_per_level),
+               "batches_visible": int(st.batches_visible),
+               "stream_bytes": int(st.stream_bytes),
+               "frac_of_measured_hbm": round(int(st.stream_bytes) / ms / 1e6 / peak, 4),
+               "octree_write_s": round(write_s, 2), "open_load_s": round(load_s, 3),
+               "what": "cr_potree_open + cr_potree_load (host encode, upload) then loop_nodes frames; "
+                       "the level-4 cut drops nodes that project below 80 px"}
+        fb.close()
+        cloud.close()
+        o.close()
+        return out
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
 
 
 def multiview_64(ctx, sh, steps, payload):

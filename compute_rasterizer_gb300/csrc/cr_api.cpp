@@ -31,6 +31,8 @@ struct cr_ctx {
     cr::FileRec* files = nullptr;  // per-file records of the frame's view (clouds > 8 files)
     int32_t files_cap = 0;
     int64_t last_dispatched = 0;  // batch records the last cull looked at
+    int64_t last_list_cap = 0;    // words of its item-list region
+    bool last_node_slices = false;
     std::vector<cr_frame_events> timing;  // GLTimerQueries-style event pairs
     int32_t timing_used = 0;
     std::string last_error;
@@ -829,12 +831,19 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     int64_t nb = loaded_batches(cloud);
     if (quirks & CR_QUIRK_DISPATCH_BY_POINTS)
         nb = std::min<int64_t>(nb, (loaded_points(cloud) + kPointsPerBatch - 1) / kPointsPerBatch);
-    s = ensure_scratch(ctx, nb);
+    // loop_nodes: nodes of up to 64,512 points go out as 10,240-point slices,
+    // so one node never holds the frame on one CTA
+    const bool slices = (quirks & CR_QUIRK_NODE_LOOP) && nb <= (int64_t)kItemNodeMask + 1;
+    const int64_t list_cap = slices ? nb * kMaxNodeSlices : nb;
+    s = ensure_scratch(ctx, list_cap);
     if (s != CR_OK) return s;
     ctx->last_dispatched = nb;
+    ctx->last_list_cap = list_cap;
+    ctx->last_node_slices = slices;
 
     CR_CUDA(ctx, cudaMemsetAsync(ctx->scratch, 0, kCounterWords * 4, st), "counter reset");
-    if (launch_cull(vp, cloud->batches, nb, cloud->capacity, quirks, ctx->scratch, stream) != 0)
+    if (launch_cull(vp, cloud->batches, nb, cloud->capacity, quirks, ctx->scratch, stream, list_cap,
+                    slices ? 1 : 0) != 0)
         return fail(ctx, CR_ERR_CUDA, "cull launch failed%s", "");
     mark(1, CR_STAGE_CULL);
 
@@ -849,7 +858,8 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     bl.depth = fb->depth;
     bl.accum = fb->accum;
     bl.scratch = ctx->scratch;
-    bl.list_cap = nb;
+    bl.list_cap = list_cap;
+    bl.node_slices = slices ? 1 : 0;
     bl.quirks = quirks;
     bl.payload = hqs ? CR_PAYLOAD_INDEX : p->payload;
     // 128 threads per CTA measured fastest for every payload at 1B points
@@ -893,7 +903,7 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
                                 cudaMemcpyDeviceToHost), "item read");
     if (n_back)  // the 20/30-bit list fills the region from its end
         CR_CUDA(ctx, cudaMemcpy(items.data() + n_front,
-                                ctx->scratch + kScratchHead + ctx->last_dispatched - n_back,
+                                ctx->scratch + kScratchHead + ctx->last_list_cap - n_back,
                                 (size_t)n_back * 4, cudaMemcpyDeviceToHost), "item read");
     std::vector<cr_batch> recs((size_t)cloud->nb);
     if (cloud->nb)
@@ -903,9 +913,10 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
     const bool hqs = p->method == CR_METHOD_LOOP_LAS_HQS;
     const bool color = hqs || p->payload == CR_PAYLOAD_COLOR;
     out->batches_dispatched = ctx->last_dispatched;
-    out->batches_visible = count;
+    out->batches_visible = 0;
     for (uint32_t it : items) {
-        const uint32_t b = it & kItemBatchMask;
+        const uint32_t b = it & (ctx->last_node_slices ? kItemNodeMask : kItemBatchMask);
+        const int64_t slice = ctx->last_node_slices ? (int64_t)((it >> kItemSliceShift) & 7u) : 0;
         const int level = (int)(it >> 29);
         if (b >= recs.size() || level > 4) continue;
         int64_t n = recs[b].num_points;
@@ -915,11 +926,16 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
         } else {
             n = std::min<int64_t>(n + ((quirks & CR_QUIRK_INCLUSIVE_END) ? 1 : 0), kPointsPerBatch);
         }
+        if (ctx->last_node_slices)  // this item's slice of the node
+            n = std::min<int64_t>(n - slice * kPointsPerBatch, kPointsPerBatch);
         const int words = level >= 2 ? 1 : (level == 1 ? 2 : 3);
-        out->batches_per_level[level] += 1;
+        if (slice == 0) {
+            out->batches_visible += 1;
+            out->batches_per_level[level] += 1;
+        }
         out->points_per_level[level] += n;
         // HQS reads the coordinates twice (depth and color pass) and colors once
-        out->stream_bytes += (hqs ? 2 : 1) * (4 * words * n + 64) + (color ? 4 * n : 0);
+        out->stream_bytes += (hqs ? 2 : 1) * (4 * words * n + (slice == 0 ? 64 : 0)) + (color ? 4 * n : 0);
     }
     return CR_OK;
 }

@@ -37,6 +37,12 @@ constexpr int64_t kStreamPad = 64;
 constexpr uint32_t kItemBatchMask = 0x0FFFFFFFu;
 constexpr uint32_t kItemWSafe = 1u << 28;
 constexpr int64_t kMaxBatches = (int64_t)1 << 28;
+// With node slicing (loop_nodes, whose nodes hold up to 64,512 points), a
+// node is handed out as items of kPointsPerBatch-point slices: the slice in
+// bits 25-27 and the node's record index below.
+constexpr int kItemSliceShift = 25;
+constexpr uint32_t kItemNodeMask = (1u << kItemSliceShift) - 1u;
+constexpr int kMaxNodeSlices = 7;
 
 // Device error bits (ctx scratch word kErrWord).
 enum : uint32_t {
@@ -96,10 +102,11 @@ struct BatchedLaunch {
     uint32_t* depth;       // HQS depth
     uint64_t* accum;       // HQS accumulators
     uint32_t* scratch;     // counters + item lists
-    int64_t list_cap;      // words of the item-list region (batch records dispatched)
+    int64_t list_cap;      // words of the item-list region
     int32_t quirks;
     int32_t payload;
     int32_t mode;
+    int32_t node_slices;   // items are node slices (see kItemSliceShift)
 };
 
 // Host-callable launchers (cr_kernels.cu).
@@ -108,8 +115,11 @@ struct BatchedLaunch {
 // parameters, 1024 files per launch) into out[0, nfiles).
 int launch_file_records(const double view[16], const double proj[16], const double* box_min,
                         int32_t nfiles, FileRec* out, void* stream, int float_uniforms = 0);
+// list_cap: words of the item-list region (nb_dispatch, or nb_dispatch *
+// kMaxNodeSlices with node_slices).
 int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb_dispatch,
-                int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream);
+                int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream,
+                int64_t list_cap = -1, int node_slices = 0);
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
                    void* stream);
 // variant 0: early-z, 1: dedup, 2: early-z & reduce (the three plain methods)

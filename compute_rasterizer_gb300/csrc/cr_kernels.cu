@@ -79,10 +79,11 @@ __device__ __forceinline__ void load_transform(const float* T, BatchCtx& c) {
 __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams vp,
                                               const cr_batch* __restrict__ batches, int64_t nb,
                                               int64_t capacity, int32_t quirks,
-                                              uint32_t* __restrict__ scratch) {
+                                              uint32_t* __restrict__ scratch, int64_t list_cap,
+                                              int32_t node_slices) {
     int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool keep = false;
-    uint32_t item = 0;
+    uint32_t item = 0, slices = 1;
     if (b < nb) {
         const int4* r4 = reinterpret_cast<const int4*>(batches + b);
         int4 a = __ldg(r4), c = __ldg(r4 + 1), d = __ldg(r4 + 2);
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
                        (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz) ? kItemWSafe : 0u);
+                if (node_slices) slices = (uint32_t)((count + kPointsPerBatch - 1) / kPointsPerBatch);
             }
         }
     }
@@ -111,6 +113,32 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
     const bool front = keep && (item >> 29) >= 2u;
     const bool back = keep && !front;
     const uint32_t lane = lane_id();
+    if (node_slices) {
+        // a node's slices side by side: warp-wide prefix sums of the slice counts
+        uint32_t sf = front ? slices : 0u, sb = back ? slices : 0u;
+        uint32_t incf = sf, incb = sb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t uf = __shfl_up_sync(kFull, incf, o), ub = __shfl_up_sync(kFull, incb, o);
+            if (lane >= (uint32_t)o) {
+                incf += uf;
+                incb += ub;
+            }
+        }
+        const uint32_t totf = __shfl_sync(kFull, incf, 31), totb = __shfl_sync(kFull, incb, 31);
+        uint32_t basef = 0, baseb = 0;
+        if (lane == 0) {
+            if (totf) basef = atomicAdd(&scratch[kItemCount], totf);
+            if (totb) baseb = atomicAdd(&scratch[kItemCount2], totb);
+        }
+        basef = __shfl_sync(kFull, basef, 0) + incf - sf;
+        baseb = __shfl_sync(kFull, baseb, 0) + incb - sb;
+        for (uint32_t k = 0; k < sf; k++)
+            scratch[kScratchHead + basef + k] = item | (k << kItemSliceShift);
+        for (uint32_t k = 0; k < sb; k++)
+            scratch[kScratchHead + list_cap - 1 - (int64_t)(baseb + k)] = item | (k << kItemSliceShift);
+        return;
+    }
     const uint32_t below = (1u << lane) - 1u;
     const uint32_t mf = __ballot_sync(kFull, front);
     if (mf) {
@@ -126,7 +154,7 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(&scratch[kItemCount2], __popc(mb));
         base = __shfl_sync(kFull, base, leader);
-        if (back) scratch[kScratchHead + nb - 1 - (int64_t)(base + __popc(mb & below))] = item;
+        if (back) scratch[kScratchHead + list_cap - 1 - (int64_t)(base + __popc(mb & below))] = item;
     }
 }
 
@@ -399,15 +427,20 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             if (threadIdx.x == 0) s_item[buf ^ 1] = atomicAdd(cursor, 1u);
             const uint32_t item =
                 bl.scratch[kScratchHead + (LIST == 0 ? (int64_t)wi : bl.list_cap - 1 - (int64_t)wi)];
-            const uint32_t b = item & kItemBatchMask;
+            const uint32_t b = item & (bl.node_slices ? kItemNodeMask : kItemBatchMask);
             const int level = (int)(item >> 29);
 
             const int4* r4 = reinterpret_cast<const int4*>(bl.batches + b);
             const int4 ra = __ldg(r4), rc = __ldg(r4 + 1), rd = __ldg(r4 + 2);
             const float mnx = __int_as_float(ra.y), mny = __int_as_float(ra.z), mnz = __int_as_float(ra.w);
             const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
-            const int64_t first = rd.x;
-            const int32_t count = (int32_t)points_in_batch(rc.w, rd.x, bl.quirks);
+            int64_t first = rd.x;
+            int32_t count = (int32_t)points_in_batch(rc.w, rd.x, bl.quirks);
+            if (bl.node_slices) {  // this item's kPointsPerBatch-point slice of the node
+                const int32_t s0 = (int32_t)((item >> kItemSliceShift) & 7u) * kPointsPerBatch;
+                first += s0;
+                count = min(count - s0, kPointsPerBatch);
+            }
             const int fi = vp.one_world ? 0 : rd.y;
             BatchCtx c;
             // render.cs:355-357, 392-394 boxSize / STEPS: a division by a power
@@ -699,10 +732,10 @@ int launch_file_records(const double view[16], const double proj[16], const doub
 }
 
 int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb, int64_t capacity,
-                int32_t quirks, uint32_t* scratch, void* stream) {
+                int32_t quirks, uint32_t* scratch, void* stream, int64_t list_cap, int node_slices) {
     if (nb <= 0) return 0;
     return launch_k(k_cull, blocks_for(nb, 256), 256, (cudaStream_t)stream, vp, batches, nb,
-                    capacity, quirks, scratch);
+                    capacity, quirks, scratch, list_cap < 0 ? nb : list_cap, (int32_t)node_slices);
 }
 
 template <int MODE, int PAYLOAD, int BLOCK, bool MANY>

@@ -606,6 +606,7 @@ def potree_nodes(ctx, sh, steps, points=10_000_000):
             ctx.render(cloud, cv, params, fb, sh)
         ctx.sync(sh)
         k = max(5, min(steps, 50))
+        ctx.timing_enable(k)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(k):
@@ -613,15 +614,19 @@ def potree_nodes(ctx, sh, steps, points=10_000_000):
         e1.record(stream)
         ctx.sync(sh)
         ms = e0.elapsed_time(e1) / k
+        stages = {name: round(float(np.mean(ctx.timing_read(v, k))), 4) for name, v in
+                  (("cull", L.STAGE_CULL), ("raster", L.STAGE_RASTER), ("resolve", L.STAGE_RESOLVE))}
+        ctx.timing_enable(0)
         st = ctx.frame_stats(cloud, params)
         peak, _ = measured_peaks()
         out = {"points": n, "nodes": len(nodes), "levels": int(max(nd["level"] for nd in nodes)) + 1,
                "max_node_points": int(max(nd["num_points"] for nd in nodes)),
                "ms_per_frame": round(ms, 4), "gpoints_per_s": round(n / ms / 1e6, 2),
+               "stages_ms": stages,
                "points_per_level": list(st.points_per_level),
                "batches_visible": int(st.batches_visible),
                "stream_bytes": int(st.stream_bytes),
-               "frac_of_measured_hbm": round(int(st.stream_bytes) / ms / 1e6 / peak, 4),
+               "raster_frac_of_measured_hbm": round(int(st.stream_bytes) / stages["raster"] / 1e6 / peak, 4),
                "octree_write_s": round(write_s, 2), "open_load_s": round(load_s, 3),
                "what": "cr_potree_open + cr_potree_load (host encode, upload) then loop_nodes frames; "
                        "the level-4 cut drops nodes that project below 80 px"}

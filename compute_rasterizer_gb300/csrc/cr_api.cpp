@@ -831,8 +831,8 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
     int64_t nb = loaded_batches(cloud);
     if (quirks & CR_QUIRK_DISPATCH_BY_POINTS)
         nb = std::min<int64_t>(nb, (loaded_points(cloud) + kPointsPerBatch - 1) / kPointsPerBatch);
-    // loop_nodes: nodes of up to 64,512 points go out as 10,240-point slices,
-    // so one node never holds the frame on one CTA
+    // loop_nodes: nodes of up to 64,512 points go out as kNodeSlice-point
+    // slices, so a frame's few hundred nodes keep every SM busy
     const bool slices = (quirks & CR_QUIRK_NODE_LOOP) && nb <= (int64_t)kItemNodeMask + 1;
     const int64_t list_cap = slices ? nb * kMaxNodeSlices : nb;
     s = ensure_scratch(ctx, list_cap);
@@ -916,7 +916,7 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
     out->batches_visible = 0;
     for (uint32_t it : items) {
         const uint32_t b = it & (ctx->last_node_slices ? kItemNodeMask : kItemBatchMask);
-        const int64_t slice = ctx->last_node_slices ? (int64_t)((it >> kItemSliceShift) & 7u) : 0;
+        const int64_t slice = ctx->last_node_slices ? (int64_t)((it >> kItemSliceShift) & 31u) : 0;
         const int level = (int)(it >> 29);
         if (b >= recs.size() || level > 4) continue;
         int64_t n = recs[b].num_points;
@@ -927,7 +927,7 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
             n = std::min<int64_t>(n + ((quirks & CR_QUIRK_INCLUSIVE_END) ? 1 : 0), kPointsPerBatch);
         }
         if (ctx->last_node_slices)  // this item's slice of the node
-            n = std::min<int64_t>(n - slice * kPointsPerBatch, kPointsPerBatch);
+            n = std::min<int64_t>(n - slice * kNodeSlice, kNodeSlice);
         const int words = level >= 2 ? 1 : (level == 1 ? 2 : 3);
         if (slice == 0) {
             out->batches_visible += 1;

@@ -38,11 +38,13 @@ constexpr uint32_t kItemBatchMask = 0x0FFFFFFFu;
 constexpr uint32_t kItemWSafe = 1u << 28;
 constexpr int64_t kMaxBatches = (int64_t)1 << 28;
 // With node slicing (loop_nodes, whose nodes hold up to 64,512 points), a
-// node is handed out as items of kPointsPerBatch-point slices: the slice in
-// bits 25-27 and the node's record index below.
-constexpr int kItemSliceShift = 25;
+// node is handed out as items of kNodeSlice points: the slice in bits 23-27
+// and the node's record index below.  Slices far smaller than a node spread
+// the few hundred visible nodes of a typical octree frame over every SM.
+constexpr int kNodeSlice = 2560;
+constexpr int kItemSliceShift = 23;
 constexpr uint32_t kItemNodeMask = (1u << kItemSliceShift) - 1u;
-constexpr int kMaxNodeSlices = 7;
+constexpr int kMaxNodeSlices = 26;  // ceil(64,512 / kNodeSlice)
 
 // Device error bits (ctx scratch word kErrWord).
 enum : uint32_t {

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
                        (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz) ? kItemWSafe : 0u);
-                if (node_slices) slices = (uint32_t)((count + kPointsPerBatch - 1) / kPointsPerBatch);
+                if (node_slices) slices = (uint32_t)((count + kNodeSlice - 1) / kNodeSlice);
             }
         }
     }
@@ -436,10 +436,10 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             const float mxx = __int_as_float(rc.x), mxy = __int_as_float(rc.y), mxz = __int_as_float(rc.z);
             int64_t first = rd.x;
             int32_t count = (int32_t)points_in_batch(rc.w, rd.x, bl.quirks);
-            if (bl.node_slices) {  // this item's kPointsPerBatch-point slice of the node
-                const int32_t s0 = (int32_t)((item >> kItemSliceShift) & 7u) * kPointsPerBatch;
+            if (bl.node_slices) {  // this item's slice of the node
+                const int32_t s0 = (int32_t)((item >> kItemSliceShift) & 31u) * kNodeSlice;
                 first += s0;
-                count = min(count - s0, kPointsPerBatch);
+                count = min(count - s0, kNodeSlice);
             }
             const int fi = vp.one_world ? 0 : rd.y;
             BatchCtx c;
@@ -462,10 +462,13 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             // full, vector-aligned batches whose w range is proven safe (nearly
             // all) skip the per-point range test and decode in pairs; the rest
             // take the general body
-            if (LIST == 0 && (item & kItemWSafe) && count == kPointsPerBatch && (first & 3) == 0 &&
-                pair_batch_exact(c))
-                run_points<MODE, PAYLOAD, BLOCK, 2, true, true>(bl, s_zc, c, pp, first,
-                                                                kPointsPerBatch, l0_x12);
+            // (node slices of kNodeSlice points qualify too: whole vectors for
+            // every thread, as the full path needs)
+            if (LIST == 0 && (item & kItemWSafe) &&
+                (count == kPointsPerBatch ||
+                 (kNodeSlice % (4 * BLOCK) == 0 && bl.node_slices && count == kNodeSlice)) &&
+                (first & 3) == 0 && pair_batch_exact(c))
+                run_points<MODE, PAYLOAD, BLOCK, 2, true, true>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, pp, first, count, l0_x12);
             else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, pp, first, count, l0_x12);

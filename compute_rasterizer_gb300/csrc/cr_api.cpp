@@ -926,8 +926,10 @@ cr_status cr_last_frame_stats(cr_ctx* ctx, const cr_cloud* cloud, const cr_rende
         } else {
             n = std::min<int64_t>(n + ((quirks & CR_QUIRK_INCLUSIVE_END) ? 1 : 0), kPointsPerBatch);
         }
-        if (ctx->last_node_slices)  // this item's slice of the node
-            n = std::min<int64_t>(n - slice * kNodeSlice, kNodeSlice);
+        if (ctx->last_node_slices) {  // this item's slice of the node
+            int64_t sf = 0;
+            node_slice(recs[b].first_point, n, slice, &sf, &n);
+        }
         const int words = level >= 2 ? 1 : (level == 1 ? 2 : 3);
         if (slice == 0) {
             out->batches_visible += 1;

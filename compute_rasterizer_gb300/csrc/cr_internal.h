@@ -2,6 +2,8 @@
 // CUDA kernels (cr_kernels.cu, cr_synth.cu).  Not part of the C ABI.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include <nvtx3/nvToolsExt.h>
@@ -41,10 +43,27 @@ constexpr int64_t kMaxBatches = (int64_t)1 << 28;
 // node is handed out as items of kNodeSlice points: the slice in bits 23-27
 // and the node's record index below.  Slices far smaller than a node spread
 // the few hundred visible nodes of a typical octree frame over every SM.
+// Slice boundaries sit at the node's first point rounded down to a 4-point
+// vector plus multiples of kNodeSlice, so every slice but the first starts on
+// a whole vector (node_slice()).
 constexpr int kNodeSlice = 2560;
 constexpr int kItemSliceShift = 23;
 constexpr uint32_t kItemNodeMask = (1u << kItemSliceShift) - 1u;
-constexpr int kMaxNodeSlices = 26;  // ceil(64,512 / kNodeSlice)
+constexpr int kMaxNodeSlices = 26;  // ceil((64,512 + 3) / kNodeSlice)
+
+// Points [*first, *first + *count) of slice `slice` of a node of `count`
+// points from `first` (host and device).
+__host__ __device__ inline void node_slice(int64_t first, int64_t count, int64_t slice, int64_t* s_first,
+                                          int64_t* s_count) {
+    const int64_t base = (first & ~(int64_t)3) + slice * kNodeSlice;
+    const int64_t lo = base > first ? base : first;
+    const int64_t hi = base + kNodeSlice < first + count ? base + kNodeSlice : first + count;
+    *s_first = lo;
+    *s_count = hi > lo ? hi - lo : 0;
+}
+__host__ __device__ inline int64_t node_slices(int64_t first, int64_t count) {
+    return count > 0 ? ((first & 3) + count + kNodeSlice - 1) / kNodeSlice : 0;
+}
 
 // Device error bits (ctx scratch word kErrWord).
 enum : uint32_t {

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
                        (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz) ? kItemWSafe : 0u);
-                if (node_slices) slices = (uint32_t)((count + kNodeSlice - 1) / kNodeSlice);
+                if (node_slices) slices = (uint32_t)cr::node_slices(fp, count);
             }
         }
     }
@@ -437,9 +437,10 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             int64_t first = rd.x;
             int32_t count = (int32_t)points_in_batch(rc.w, rd.x, bl.quirks);
             if (bl.node_slices) {  // this item's slice of the node
-                const int32_t s0 = (int32_t)((item >> kItemSliceShift) & 31u) * kNodeSlice;
-                first += s0;
-                count = min(count - s0, kNodeSlice);
+                int64_t sf, sc;
+                node_slice(first, count, (item >> kItemSliceShift) & 31u, &sf, &sc);
+                first = sf;
+                count = (int32_t)sc;
             }
             const int fi = vp.one_world ? 0 : rd.y;
             BatchCtx c;

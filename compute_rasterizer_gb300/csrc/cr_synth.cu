@@ -204,7 +204,7 @@ __host__ __device__ inline uint64_t spread3(uint32_t a) {
 
 struct MortonFrame {
     double min[3];
-    double cube;
+    double cube, inv;  // inv = RN(1 / cube)
     double scale[3];
     double offset[3];
 };
@@ -212,12 +212,20 @@ struct MortonFrame {
 // Sort_Frugal/src/main.cpp:82-105: normalise by the largest header extent.
 // The tool passes 2^21 for a point on the cube's far face to a 21-bit mask,
 // which wraps it to 0 and sorts it to the front; it is clamped to 2^21 - 1 here.
+// uint32(((v - min) / cube) * 2^21) as one product with the reciprocal: d *
+// inv lies within a few ulps of RN(d / cube), so when no integer lies within
+// 16 ulps of t1 = d * inv * 2^21 both truncate to the same integer; otherwise
+// (rarely) the division is done.  Same rule as the encoder's quantize30.
 __host__ __device__ inline uint64_t morton_of(const MortonFrame& f, const uint8_t* rec) {
     uint32_t q[3];
     for (int k = 0; k < 3; k++) {
         const double v = (double)get_i32(rec + 4 * k) * f.scale[k] + f.offset[k];
-        const double nv = (v - f.min[k]) / f.cube;
-        const uint32_t u = (uint32_t)(nv * 2097152.0);
+        const double d = v - f.min[k];
+        const double t1 = (d * f.inv) * 2097152.0;
+        const double e = t1 * 0x1p-49;
+        double t = t1;
+        if (!(floor(t1 - e) == floor(t1 + e))) t = (d / f.cube) * 2097152.0;
+        const uint32_t u = (t >= 0.0) ? (t < 4294967295.0 ? (uint32_t)t : 0xFFFFFFFFu) : 0u;
         q[k] = u < 2097151u ? u : 2097151u;
     }
     return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
@@ -234,6 +242,7 @@ MortonFrame morton_frame(const cr_las_header* h) {
     }
     f.cube = std::max(std::max(size[0], size[1]), size[2]);
     if (!(f.cube > 0.0)) f.cube = 1.0;
+    f.inv = 1.0 / f.cube;
     return f;
 }
 

@@ -18,6 +18,7 @@
 
 #include "../../include/cr_synth.h"
 #include "cr_internal.h"
+#include "cr_quant.h"
 
 namespace {
 
@@ -207,6 +208,7 @@ struct MortonFrame {
     double cube, inv;  // inv = RN(1 / cube)
     double scale[3];
     double offset[3];
+    cr::QuantFx fx[3];  // the GPU keys' integer form of morton_axis (cr_quant.h)
 };
 
 // Sort_Frugal/src/main.cpp:82-105: normalise by the largest header extent.
@@ -216,17 +218,32 @@ struct MortonFrame {
 // inv lies within a few ulps of RN(d / cube), so when no integer lies within
 // 16 ulps of t1 = d * inv * 2^21 both truncate to the same integer; otherwise
 // (rarely) the division is done.  Same rule as the encoder's quantize30.
+__host__ __device__ inline uint32_t morton_axis(const MortonFrame& f, int k, int32_t X) {
+    const double v = (double)X * f.scale[k] + f.offset[k];
+    const double d = v - f.min[k];
+    const double t1 = (d * f.inv) * 2097152.0;
+    const double e = t1 * 0x1p-49;
+    double t = t1;
+    if (!(floor(t1 - e) == floor(t1 + e))) t = (d / f.cube) * 2097152.0;
+    const uint32_t u = (t >= 0.0) ? (t < 4294967295.0 ? (uint32_t)t : 0xFFFFFFFFu) : 0u;
+    return u < 2097151u ? u : 2097151u;
+}
+
 __host__ __device__ inline uint64_t morton_of(const MortonFrame& f, const uint8_t* rec) {
     uint32_t q[3];
+    for (int k = 0; k < 3; k++) q[k] = morton_axis(f, k, get_i32(rec + 4 * k));
+    return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+}
+
+// The GPU keys: the cell in integer arithmetic where the error bound decides
+// it (all but about one point in 10^5 per axis for LAS scales and extents),
+// else the double chain.  The host sort keeps the chain, so every GPU/host
+// comparison checks the integer form.
+__device__ inline uint64_t morton_of_fast(const MortonFrame& f, const uint8_t* rec) {
+    uint32_t q[3];
     for (int k = 0; k < 3; k++) {
-        const double v = (double)get_i32(rec + 4 * k) * f.scale[k] + f.offset[k];
-        const double d = v - f.min[k];
-        const double t1 = (d * f.inv) * 2097152.0;
-        const double e = t1 * 0x1p-49;
-        double t = t1;
-        if (!(floor(t1 - e) == floor(t1 + e))) t = (d / f.cube) * 2097152.0;
-        const uint32_t u = (t >= 0.0) ? (t < 4294967295.0 ? (uint32_t)t : 0xFFFFFFFFu) : 0u;
-        q[k] = u < 2097151u ? u : 2097151u;
+        const int32_t X = get_i32(rec + 4 * k);
+        if (!cr::quant_fast(f.fx[k], X, 2097151u, &q[k])) q[k] = morton_axis(f, k, X);
     }
     return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
 }
@@ -243,6 +260,8 @@ MortonFrame morton_frame(const cr_las_header* h) {
     f.cube = std::max(std::max(size[0], size[1]), size[2]);
     if (!(f.cube > 0.0)) f.cube = 1.0;
     f.inv = 1.0 / f.cube;
+    for (int k = 0; k < 3; k++)
+        f.fx[k] = cr::quant_setup(f.scale[k], f.offset[k], f.min[k], 0.0, false, f.cube, 21, INT32_MIN, INT32_MAX);
     return f;
 }
 
@@ -301,7 +320,7 @@ __global__ void k_morton_keys(MortonFrame f, const uint8_t* rec, int64_t n, int3
                               unsigned long long* keys, uint32_t* idx) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        keys[i] = morton_of(f, rec + i * bpp);
+        keys[i] = morton_of_fast(f, rec + i * bpp);
         idx[i] = (uint32_t)i;
     }
 }
@@ -372,6 +391,7 @@ __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __r
                                                 uint32_t* hi, uint32_t* rgba) {
     __shared__ int32_t s_red[6][8];
     __shared__ double s_box[9];
+    __shared__ cr::QuantFx s_fx[3];
     const int64_t first = (int64_t)blockIdx.x * cr::kPointsPerBatch;
     const int64_t left = a.n - first;
     const int cnt = (int)(left < cr::kPointsPerBatch ? left : cr::kPointsPerBatch);
@@ -412,6 +432,7 @@ __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __r
         s_box[k] = b0;
         s_box[3 + k] = b1;
         s_box[6 + k] = 1.0 / (b1 - b0);
+        s_fx[k] = cr::quant_setup(a.scale[k], a.offset[k], a.box_min[k], b0, true, b1 - b0, 30, lo, hi);
     }
     __syncthreads();
     const double bmin[3] = {s_box[0], s_box[1], s_box[2]};
@@ -427,13 +448,18 @@ __global__ void __launch_bounds__(256) k_encode(EncodeArgs a, const uint8_t* __r
         b.file_index = a.file_index;
         batches[blockIdx.x] = b;
     }
+    // Each coordinate's 30-bit cell in integer arithmetic where the error bound
+    // decides it (cr_quant.h), else the double chain: the same integer either way.
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
         const int64_t pi = first + i;
         const uint8_t* r = rec + pi * a.bpp;
         uint32_t q[3];
         for (int k = 0; k < 3; k++) {
-            const double v = (double)get_i32(r + 4 * k) * a.scale[k] + a.offset[k] - a.box_min[k];
-            q[k] = quantize30(v - bmin[k], size[k], inv[k]);
+            const int32_t X = get_i32(r + 4 * k);
+            if (!cr::quant_fast(s_fx[k], X, 1073741823u, &q[k])) {
+                const double v = (double)X * a.scale[k] + a.offset[k] - a.box_min[k];
+                q[k] = quantize30(v - bmin[k], size[k], inv[k]);
+            }
         }
         lo[pi] = ((q[0] >> 20) & 1023u) | (((q[1] >> 20) & 1023u) << 10) | (((q[2] >> 20) & 1023u) << 20);
         md[pi] = ((q[0] >> 10) & 1023u) | (((q[1] >> 10) & 1023u) << 10) | (((q[2] >> 10) & 1023u) << 20);

@@ -296,6 +296,7 @@ struct PairParams {
     uint64_t T[9];          // (T[k], T[k]) for T0, T1, T3, T4, T5, T7, T8, T9, T11
     uint64_t half, Wf, Hf;  // (0.5, 0.5), (W, W), (H, H)
     uint64_t bias;          // (-2^23, -2^23)
+    uint64_t one, nhalf;    // (1, 1), (-0.5, -0.5)
 };
 struct PairCol3 {
     uint64_t T12, T13, T15;  // the batch's file's translation column, as pairs
@@ -325,6 +326,23 @@ __device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
 }
 
+// -RN(1/w) for both elements of a pair, |w| in [2^-126, 2^126): the Newton
+// step of rcp_rn_normal done once for the pair.  NY holds the approximations
+// of -1/w (rcp.approx of -w); E = fma(w, NY, 1) = 1 - w*y is exact, and
+// fma(E, NY, NY) = -(y + E*y) rounds to -RN(1/w), rounding to nearest being
+// symmetric.  The negated result spares negating a pair (the callers fold the
+// sign into their next operation); cr_check_reciprocal runs this form against
+// __frcp_rn over every float in the range.  On the raster (1B points):
+// index payload 1.408 -> 1.353 ms, HQS 3.425 -> 3.334 ms, color 1.562 -> 1.554 ms.
+__device__ __forceinline__ uint64_t f2_neg_rcp_rn_normal(uint64_t W, uint64_t one) {
+    float w0, w1, n0, n1;
+    f2_unpack(W, w0, w1);
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(n0) : "f"(-w0));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(n1) : "f"(-w1));
+    const uint64_t NY = f2_pack(n0, n1);
+    return f2_fma(f2_fma(W, NY, one), NY, NY);
+}
+
 // A batch's 10-bit decode uniforms as pairs (per batch, in registers): the
 // steps sx, sy * 2^-10, sz * 2^-20 and the minimum corner (see project_pair10).
 struct PairBatch {
@@ -342,27 +360,27 @@ __device__ __forceinline__ bool pair_batch_exact(const BatchCtx& c) {
            fmul(fmul(c.sz, 0x1p-20f), 0x1p20f) == c.sz;
 }
 
-// project_finish() for two points: clip positions (PX, PY, PW) as pairs, the
-// uniforms half = (0.5, 0.5), Wf = (W, W), Hf = (H, H).
+// project_finish() for two points: clip positions (PX, PY, PW) as pairs.  The
+// pair quotients come out negated (NQ = -q, from -RN(1/w)): the inside test is
+// symmetric, and q * 0.5 + 0.5 is the same real value as NQ * -0.5 + 0.5, so
+// every result is the scalar path's.
 __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, uint64_t PW,
-                                                    uint64_t half, uint64_t Wf, uint64_t Hf,
-                                                    int32_t W, bool ok[2], int32_t pix[2],
-                                                    uint32_t wbits[2]) {
-    float pw[2];
-    f2_unpack(PW, pw[0], pw[1]);
+                                                    const PairParams& pp, int32_t W, bool ok[2],
+                                                    int32_t pix[2], uint32_t wbits[2]) {
     // callers: w-safe batches only (every w in [2^-120, 2^120])
-    const uint64_t R = f2_pack(rcp_rn_normal(pw[0]), rcp_rn_normal(pw[1]));
-    const uint64_t QX = f2_mul(PX, R), QY = f2_mul(PY, R);
-    const uint64_t FX = f2_mul(f2_fma(QX, half, half), Wf);
-    const uint64_t FY = f2_mul(f2_fma(QY, half, half), Hf);
-    float qx[2], qy[2], fx[2], fy[2];
-    f2_unpack(QX, qx[0], qx[1]);
-    f2_unpack(QY, qy[0], qy[1]);
+    const uint64_t NR = f2_neg_rcp_rn_normal(PW, pp.one);
+    const uint64_t NQX = f2_mul(PX, NR), NQY = f2_mul(PY, NR);
+    const uint64_t FX = f2_mul(f2_fma(NQX, pp.nhalf, pp.half), pp.Wf);
+    const uint64_t FY = f2_mul(f2_fma(NQY, pp.nhalf, pp.half), pp.Hf);
+    float pw[2], nqx[2], nqy[2], fx[2], fy[2];
+    f2_unpack(PW, pw[0], pw[1]);
+    f2_unpack(NQX, nqx[0], nqx[1]);
+    f2_unpack(NQY, nqy[0], nqy[1]);
     f2_unpack(FX, fx[0], fx[1]);
     f2_unpack(FY, fy[0], fy[1]);
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-        ok[k] = pw[k] > 0.0f && qx[k] >= -1.0f && qx[k] <= 1.0f && qy[k] >= -1.0f && qy[k] <= 1.0f;
+        ok[k] = pw[k] > 0.0f && nqx[k] >= -1.0f && nqx[k] <= 1.0f && nqy[k] >= -1.0f && nqy[k] <= 1.0f;
         pix[k] = small_f2i(fx[k]) + small_f2i(fy[k]) * W;
         wbits[k] = __float_as_uint(pw[k]);
     }
@@ -394,7 +412,7 @@ __device__ __forceinline__ void project_pair10(const PairParams& pp, const PairC
     const uint64_t PX = f2_fma(pp.T[6], Z, f2_fma(pp.T[3], Y, f2_fma(pp.T[0], X, f.T12)));
     const uint64_t PY = f2_fma(pp.T[7], Z, f2_fma(pp.T[4], Y, f2_fma(pp.T[1], X, f.T13)));
     const uint64_t PW = f2_fma(pp.T[8], Z, f2_fma(pp.T[5], Y, f2_fma(pp.T[2], X, f.T15)));
-    project_pair_finish(PX, PY, PW, pp.half, pp.Wf, pp.Hf, W, ok, pix, wbits);
+    project_pair_finish(PX, PY, PW, pp, W, ok, pix, wbits);
 }
 
 // Host side: the pair uniforms of a view (file 0's columns 0-2, which every
@@ -411,6 +429,8 @@ inline void fill_pair_params(const ViewParams& vp, PairParams* pp) {
     pp->bias = dup(-8388608.0f);
     pp->Wf = dup((float)vp.W);
     pp->Hf = dup((float)vp.H);
+    pp->one = dup(1.0f);
+    pp->nhalf = dup(-0.5f);
 }
 
 }  // namespace

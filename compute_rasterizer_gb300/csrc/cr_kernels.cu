@@ -703,7 +703,15 @@ __global__ void __launch_bounds__(256) k_check_reciprocal(unsigned long long* ba
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (1ull << 32); i += stride) {
         const float x = __uint_as_float((uint32_t)i);
         const float a = rcp_rn(x), b = __frcp_rn(x);
-        if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) {
+        bool bad_x = __float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b);
+        // the pair form of the w-safe batches, on (x, -x): (-RN(1/x), RN(1/x))
+        if ((((uint32_t)i & 0x7FFFFFFFu) - 0x00800000u) < 0x7E000000u) {
+            float n0, n1;
+            f2_unpack(f2_neg_rcp_rn_normal(f2_pack(x, -x), f2_pack(1.0f, 1.0f)), n0, n1);
+            bad_x = bad_x || __float_as_uint(n0) != (__float_as_uint(b) ^ 0x80000000u) ||
+                    __float_as_uint(n1) != __float_as_uint(b);
+        }
+        if (bad_x) {
             mine++;
             atomicMin(first, (uint32_t)i);
         }

@@ -261,8 +261,9 @@ __device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, floa
     const float rw = SAFE ? rcp_rn_normal(pw) : rcp_rn(pw);
     float qx = fmul(px, rw), qy = fmul(py, rw);
     // render.cs:404 written positively, so a NaN position is outside (the
-    // negated form would keep it and index the framebuffer with garbage)
-    bool in = pw > 0.0f && qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f;
+    // negated form would keep it and index the framebuffer with garbage); in
+    // w-safe batches w >= 2^-120 at every point, so w > 0 needs no test
+    bool in = (SAFE || pw > 0.0f) && qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f;
     int32_t ix = small_f2i(fmul(__fmaf_rn(qx, 0.5f, 0.5f), c.Wf));
     int32_t iy = small_f2i(fmul(__fmaf_rn(qy, 0.5f, 0.5f), c.Hf));
     pix = ix + iy * c.W;
@@ -380,7 +381,9 @@ __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, ui
     f2_unpack(FY, fy[0], fy[1]);
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-        ok[k] = pw[k] > 0.0f && nqx[k] >= -1.0f && nqx[k] <= 1.0f && nqy[k] >= -1.0f && nqy[k] <= 1.0f;
+        // w >= 2^-120 for every point of a w-safe batch: render.cs:404's w > 0
+        // holds, so only the x and y bounds are tested (HQS 3.334 -> 3.281 ms)
+        ok[k] = nqx[k] >= -1.0f && nqx[k] <= 1.0f && nqy[k] >= -1.0f && nqy[k] <= 1.0f;
         pix[k] = small_f2i(fx[k]) + small_f2i(fy[k]) * W;
         wbits[k] = __float_as_uint(pw[k]);
     }

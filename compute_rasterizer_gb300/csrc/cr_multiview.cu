@@ -260,7 +260,7 @@ __device__ __forceinline__ void splat_pair(const MVArgs& a, unsigned long long* 
         const float pw = __fmaf_rn(aT11, z, __fmaf_rn(aT7, y, __fmaf_rn(aT3, x, aT15)));
         const float rw = SAFE ? rcp_rn_normal(pw) : rcp_rn(pw);
         const float qy = fmul(py, rw);
-        const bool yin = ((valid_mask >> j) & 1u) && pw > 0.0f && qy >= -1.0f && qy <= 1.0f;
+        const bool yin = ((valid_mask >> j) & 1u) && (SAFE || pw > 0.0f) && qy >= -1.0f && qy <= 1.0f;
         const int32_t row = small_f2i(fmul(__fmaf_rn(qy, 0.5f, 0.5f), Hf)) * W;
         const uint32_t wbits = __float_as_uint(pw);
         const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? u4get(col, j) : idx0 + (uint32_t)j;

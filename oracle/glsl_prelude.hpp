@@ -1,0 +1,65 @@
+// glsl_prelude.hpp -- the GLSL compute-shader environment a reference shader
+// needs to compile as C++ (TEST INFRASTRUCTURE: included only by the
+// translations oracle/glsl_cpp.py writes into oracle/_ref/, which the CPU
+// tests run as the reference side of a parity pin).
+//
+// Vector and matrix types, their operators and the built-in functions are the
+// reference's vendored glm (GLSL semantics in C++, swizzles enabled).  A
+// workgroup's invocations run one after another; the translated shaders use
+// no barrier, shared memory or subgroup operation, so that order is one the
+// GPU could have produced, and every atomic below is a plain read-modify-write.
+// Floating point is IEEE binary32 without contraction (-ffp-contract=off):
+// each GLSL operation rounds once, a vector divided by a scalar divides each
+// component, and glm's matrix products keep glm's association.
+#pragma once
+
+#define GLM_FORCE_SWIZZLE
+#include <array>
+#include <cstdint>
+#include <glm/glm.hpp>
+
+// A swizzle combined with a scalar by + or / (`p.xy / p.w`, `p.xy + 1.0`; glm
+// itself defines - and *): the swizzled vector's operator, element by
+// element as GLSL defines it.
+namespace glm {
+namespace detail {
+#define CR_GLSL_SWIZZLE_SCALAR_OP(OP)                                                            \
+    template <int N, typename T, precision P, template <typename, precision> class V, int E0,   \
+              int E1, int E2, int E3>                                                            \
+    inline V<T, P> operator OP(_swizzle<N, T, P, V, E0, E1, E2, E3> const& a, T const& b) {     \
+        return a() OP b;                                                                         \
+    }                                                                                            \
+    template <int N, typename T, precision P, template <typename, precision> class V, int E0,   \
+              int E1, int E2, int E3>                                                            \
+    inline V<T, P> operator OP(T const& a, _swizzle<N, T, P, V, E0, E1, E2, E3> const& b) {     \
+        return a OP b();                                                                         \
+    }
+CR_GLSL_SWIZZLE_SCALAR_OP(+)
+CR_GLSL_SWIZZLE_SCALAR_OP(/)
+#undef CR_GLSL_SWIZZLE_SCALAR_OP
+}  // namespace detail
+}  // namespace glm
+
+using namespace glm;
+typedef unsigned int uint;
+
+static uvec3 gl_WorkGroupID(0u), gl_LocalInvocationID(0u), gl_GlobalInvocationID(0u);
+
+template <class T, class U>
+inline T atomicAdd(T& a, U v) {
+    const T old = a;
+    a = (T)(a + (T)v);
+    return old;
+}
+template <class T, class U>
+inline T atomicMin(T& a, U v) {
+    const T old = a;
+    if ((T)v < a) a = (T)v;
+    return old;
+}
+template <class T, class U>
+inline T atomicMax(T& a, U v) {
+    const T old = a;
+    if ((T)v > a) a = (T)v;
+    return old;
+}

@@ -159,13 +159,33 @@ void or_orbit_world(double yaw, double pitch, double radius, const double target
     memcpy(out, d, sizeof(d));
 }
 
+/* Arithmetic interpretation (or_set_arith).  OR_ARITH_CONTRACT: the contract
+ * in oracle.h, which the kernels follow.  OR_ARITH_LITERAL: the shader source
+ * evaluated operation by operation in IEEE binary32 with glm's operators --
+ * what the reference shaders compute when compiled as C++ against the
+ * reference's glm (oracle/shader_ref.cpp): mul then add in the decode,
+ * mat4 * vec4 = (m0 x + m1 y) + (m2 z + m3 w) (glm's type_mat4x4.inl), a vector
+ * divided by a scalar divides each component.  Everything else is shared. */
+static int g_arith = OR_ARITH_CONTRACT;
+int or_set_arith(int mode) {
+    const int old = g_arith;
+    g_arith = mode;
+    return old;
+}
+
 /* render.cs:134-143 createPlane + :145-174 frustumPlanes. */
 static void create_plane(float x, float y, float z, float w, float out[4]) {
     float len = sqrtf((x * x + y * y) + z * z);
-    float inv = 1.0f / len; /* vec3(x, y, z) / nLength: one reciprocal */
-    out[0] = x * inv;
-    out[1] = y * inv;
-    out[2] = z * inv;
+    if (g_arith == OR_ARITH_LITERAL) {
+        out[0] = x / len;
+        out[1] = y / len;
+        out[2] = z / len;
+    } else {
+        float inv = 1.0f / len; /* vec3(x, y, z) / nLength: one reciprocal */
+        out[0] = x * inv;
+        out[1] = y * inv;
+        out[2] = z * inv;
+    }
     out[3] = w / len;
 }
 
@@ -237,6 +257,10 @@ int or_intersects_frustum(const float planes[6][4], const float wmin[3], const f
 
 static void mat4_vec4(const float m[16], const float v[4], float o[4]) {
     for (int r = 0; r < 4; r++) {
+        if (g_arith == OR_ARITH_LITERAL) {
+            o[r] = (m[0 * 4 + r] * v[0] + m[1 * 4 + r] * v[1]) + (m[2 * 4 + r] * v[2] + m[3 * 4 + r] * v[3]);
+            continue;
+        }
         float s = m[0 * 4 + r] * v[0];
         s = s + m[1 * 4 + r] * v[1];
         s = s + m[2 * 4 + r] * v[2];
@@ -257,9 +281,15 @@ int or_precision_level(const or_frame* fr, const or_file_frame* file, const floa
     ve[0] = vc[0] + radius; ve[1] = vc[1] + 0.0f; ve[2] = vc[2] + 0.0f; ve[3] = vc[3] + 0.0f;
     mat4_vec4(fr->proj, vc, pc);
     mat4_vec4(fr->proj, ve, pe);
-    float rc = 1.0f / pc[3], re = 1.0f / pe[3]; /* xy / w: one reciprocal each */
-    float pcx = pc[0] * rc, pcy = pc[1] * rc;
-    float pex = pe[0] * re, pey = pe[1] * re;
+    float pcx, pcy, pex, pey;
+    if (g_arith == OR_ARITH_LITERAL) {
+        pcx = pc[0] / pc[3]; pcy = pc[1] / pc[3];
+        pex = pe[0] / pe[3]; pey = pe[1] / pe[3];
+    } else {
+        float rc = 1.0f / pc[3], re = 1.0f / pe[3]; /* xy / w: one reciprocal each */
+        pcx = pc[0] * rc; pcy = pc[1] * rc;
+        pex = pe[0] * re; pey = pe[1] * re;
+    }
     float W = (float)fr->width, H = (float)fr->height;
     float scx = (W * (pcx + 1.0f)) / 2.0f, scy = (H * (pcy + 1.0f)) / 2.0f;
     float sex = (W * (pex + 1.0f)) / 2.0f, sey = (H * (pey + 1.0f)) / 2.0f;
@@ -311,6 +341,12 @@ static void decode_point(const batch_decode* d, int32_t quirks, int64_t idx, con
             X |= x12; Y |= y12; Z |= z12;
         }
     }
+    if (g_arith == OR_ARITH_LITERAL) {
+        p[0] = (float)X * d->sx + d->minx;
+        p[1] = (float)Y * d->sy + d->miny;
+        p[2] = (float)Z * d->sz + d->minz;
+        return;
+    }
     p[0] = fmaf((float)X, d->sx, d->minx);
     p[1] = fmaf((float)Y, d->sy, d->miny);
     p[2] = fmaf((float)Z, d->sz, d->minz);
@@ -319,14 +355,29 @@ static void decode_point(const batch_decode* d, int32_t quirks, int64_t idx, con
 /* render.cs:399-409: returns 1 and the pixel id if the point lands inside */
 static int project(const float T[16], int32_t W, int32_t H, const float p[3], int32_t* pix,
                    float* w_out) {
-    float x = fmaf(T[8], p[2], fmaf(T[4], p[1], fmaf(T[0], p[0], T[12])));
-    float y = fmaf(T[9], p[2], fmaf(T[5], p[1], fmaf(T[1], p[0], T[13])));
-    float w = fmaf(T[11], p[2], fmaf(T[7], p[1], fmaf(T[3], p[0], T[15])));
+    const int lit = g_arith == OR_ARITH_LITERAL;
+    float x, y, w;
+    if (lit) { /* file.transform * vec4(point, 1.0) in glm's association */
+        x = (T[0] * p[0] + T[4] * p[1]) + (T[8] * p[2] + T[12] * 1.0f);
+        y = (T[1] * p[0] + T[5] * p[1]) + (T[9] * p[2] + T[13] * 1.0f);
+        w = (T[3] * p[0] + T[7] * p[1]) + (T[11] * p[2] + T[15] * 1.0f);
+    } else {
+        x = fmaf(T[8], p[2], fmaf(T[4], p[1], fmaf(T[0], p[0], T[12])));
+        y = fmaf(T[9], p[2], fmaf(T[5], p[1], fmaf(T[1], p[0], T[13])));
+        w = fmaf(T[11], p[2], fmaf(T[7], p[1], fmaf(T[3], p[0], T[15])));
+    }
     /* render.cs:404 `!(w <= 0 || x < -1 || ...)`, written positively so that
      * a NaN position counts as outside */
     if (!(w > 0.0f)) return 0;
-    float rw = 1.0f / w; /* pos.xyz / pos.w: one reciprocal of w */
-    float qx = x * rw, qy = y * rw;
+    float qx, qy;
+    if (lit) {
+        qx = x / w;
+        qy = y / w;
+    } else {
+        float rw = 1.0f / w; /* pos.xyz / pos.w: one reciprocal of w */
+        qx = x * rw;
+        qy = y * rw;
+    }
     if (!(qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f)) return 0;
     float fx = fmaf(qx, 0.5f, 0.5f) * (float)W;
     float fy = fmaf(qy, 0.5f, 0.5f) * (float)H;

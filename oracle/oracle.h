@@ -83,6 +83,16 @@ enum {
 
 enum { OR_PAYLOAD_INDEX = 0, OR_PAYLOAD_COLOR = 1 };
 
+/* Arithmetic interpretation of the shader math (oracle.c, or_set_arith):
+ * CONTRACT is the contract above (the kernels' arithmetic); LITERAL evaluates
+ * the shader source operation by operation with glm's operators, as the
+ * reference shaders compiled as C++ do (oracle/shader_ref.cpp), which pins
+ * everything but the contract's FMA and reciprocal choices to the reference's
+ * own source.  Returns the previous mode; process-wide, set it before
+ * or_file_setup and the raster calls. */
+enum { OR_ARITH_CONTRACT = 0, OR_ARITH_LITERAL = 1 };
+int or_set_arith(int mode);
+
 typedef struct or_frame {
     float proj[16];
     int32_t width, height;

@@ -16,10 +16,12 @@ LIB = HERE / "_build" / "liboracle.so"
 GLMREF = HERE / "_ref" / "libglmref.so"
 SFREF = HERE / "_ref" / "libsfref.so"
 LAZREF = HERE / "_ref" / "liblaszipref.so"
+SHADERREF = HERE / "_ref" / "libshaderref.so"
 
 L0_X12, INCLUSIVE_END, DISPATCH_BY_POINTS, UVEC4_BASE, RESOLVE_TILES = 1, 2, 4, 8, 16
 NODE_LOOP, LEVEL4_80PX, ONE_WORLD = 32, 64, 128
 PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
+ARITH_CONTRACT, ARITH_LITERAL = 0, 1
 
 
 class FileFrame(C.Structure):
@@ -87,6 +89,7 @@ def lib() -> C.CDLL:
             "or_morton3": [C.c_uint32] * 3,
             "or_fnv1a64": [P, I64],
             "or_dispatch_batches": [I64, I64, I32],
+            "or_set_arith": [C.c_int],
         }
         for k, v in sig.items():
             getattr(_lib, k).argtypes = v
@@ -96,7 +99,23 @@ def lib() -> C.CDLL:
         _lib.or_morton3.restype = C.c_uint64
         _lib.or_fnv1a64.restype = C.c_uint64
         _lib.or_dispatch_batches.restype = C.c_int64
+        _lib.or_set_arith.restype = C.c_int
     return _lib
+
+
+class arith:
+    """with arith(ARITH_LITERAL): ... -- the oracle's arithmetic interpretation
+    (oracle.h) for the frames set up and rasterized inside the block."""
+
+    def __init__(self, mode: int):
+        self.mode, self.old = int(mode), None
+
+    def __enter__(self):
+        self.old = lib().or_set_arith(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        lib().or_set_arith(self.old)
 
 
 def _p(a):
@@ -137,6 +156,16 @@ def laszipref() -> C.CDLL:
     g.lzref_compress.restype = I64
     g.lzref_decompress.argtypes = [P, I64, I64, P, C.c_int32, I64, I, P]
     g.lzref_decompress.restype = I64
+    return g
+
+
+def shaderref() -> C.CDLL:
+    """The reference's GLSL shaders translated to C++ and run on the CPU
+    (oracle/shader_ref.cpp, built into oracle/_ref)."""
+    g = C.CDLL(str(SHADERREF))
+    P, I32, I64 = C.c_void_p, C.c_int32, C.c_int64
+    g.ref_loop_las_render.argtypes = [P, I64, P, P, P, P, P, P, I32, I32, I32, I64, P]
+    g.ref_loop_las_render.restype = C.c_int
     return g
 
 

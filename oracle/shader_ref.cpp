@@ -1,0 +1,56 @@
+// shader_ref.cpp -- runs the reference's own GLSL compute shaders on the CPU
+// (TEST INFRASTRUCTURE: compiled by oracle/Makefile's `ref` target into
+// oracle/_ref/libshaderref.so, loaded only by the CPU tests as the reference
+// side of the oracle's parity pin; nothing in the product links it).
+//
+// Each shader is translated to C++ by oracle/glsl_cpp.py (written into
+// oracle/_ref/, never committed) and included here under its own namespace.
+// An entry point binds the shader's buffers and uniforms to caller arrays and
+// runs its dispatch: every workgroup, and in it every invocation, one after
+// another (the shaders use no barrier, shared memory or subgroup operation).
+// The arithmetic is the shader's own, evaluated in IEEE binary32 without
+// contraction, with glm's operators: the oracle's literal arithmetic mode.
+#include <cstring>
+
+#include "loop_las_render.cpp"
+
+extern "C" {
+
+// compute_loop_las/render.cs dispatched as compute_loop_las.h:233 does (one
+// workgroup per batch record).  files: per file the shader's File record,
+// mat4 transform, transformFrustum, world, padding (64 floats, column-major).
+int ref_loop_las_render(const void* batches, int64_t num_batches, const uint32_t* lo,
+                        const uint32_t* md, const uint32_t* hi, const void* files,
+                        const float view[16], const float proj[16], int32_t width, int32_t height,
+                        int32_t frustum_culling, int64_t num_points, uint64_t* fb) {
+    using namespace loop_las;
+    ssFramebuffer = fb;
+    ssBatches = const_cast<Batch*>(static_cast<const Batch*>(batches));
+    ssXyz_4b = const_cast<uint32_t*>(lo);
+    ssXyz_8b = const_cast<uint32_t*>(md);
+    ssXyz_12b = const_cast<uint32_t*>(hi);
+    ssRGBA = nullptr;
+    ssFiles = const_cast<File*>(static_cast<const File*>(files));
+    std::memset(&debug, 0, sizeof(debug));
+    std::memset(&boundingBoxes, 0, sizeof(boundingBoxes));
+    std::memset(&uniforms, 0, sizeof(uniforms));
+    std::memcpy(&uniforms.view[0][0], view, 16 * sizeof(float));
+    std::memcpy(&uniforms.proj[0][0], proj, 16 * sizeof(float));
+    uniforms.pointsPerThread = 80;  // compute_loop_las.h:155 (POINTS_PER_THREAD, Resources.h:4)
+    uniforms.enableFrustumCulling = frustum_culling;
+    uniforms.showBoundingBox = 0;
+    uniforms.numPoints = (int)num_points;
+    uniforms.imageSize = ivec2(width, height);
+    uniforms.colorizeChunks = false;
+    uniforms.colorizeOverdraw = false;
+    for (int64_t b = 0; b < num_batches; b++)
+        for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
+            gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
+            gl_LocalInvocationID = uvec3(t, 0u, 0u);
+            gl_GlobalInvocationID = uvec3((uint)b * gl_WorkGroupSize.x + t, 0u, 0u);
+            shader_main();
+        }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,84 @@
+"""The oracle pinned to the reference's own GLSL shaders.
+
+oracle/glsl_cpp.py translates the reference's compute shaders to C++ (the
+statements as written, glm for the GLSL types and operators) and
+oracle/shader_ref.cpp runs their dispatches on the CPU.  The oracle in its
+literal arithmetic mode (IEEE operations in the source's order, glm's
+association) must produce the same framebuffers bit for bit; the contract
+mode, which the kernels follow, differs from it only in its FMA and
+reciprocal choices, which GLSL leaves to the driver.  Skipped where the
+reference checkout is absent (the probe is built from it)."""
+import numpy as np
+import pytest
+
+from compute_rasterizer_gb300 import _lib as L
+from helpers import cameras, encoded, many_file_cameras, many_file_cloud, oracle_frame
+from oracle import oracle as O
+
+pytestmark = pytest.mark.skipif(not O.SHADERREF.exists(),
+                                reason="no reference checkout: shader probe not built")
+
+
+def shader_files(fr, box_mins):
+    """The shaders' File records (render.cs:44-49): transform, transformFrustum,
+    world = translate(boxMin), padding; compute_loop_las.h:166-200."""
+    files = np.zeros((len(box_mins), 64), np.float32)
+    for i, bm in enumerate(np.asarray(box_mins, np.float64).reshape(-1, 3)):
+        t = np.frombuffer(bytes(fr.files[i].transform), np.float32)
+        files[i, :16] = t
+        files[i, 16:32] = t
+        world = np.eye(4)
+        world[3, :3] = bm
+        files[i, 32:48] = world.reshape(16).astype(np.float32)
+    return files
+
+
+def f32(m):
+    return np.ascontiguousarray(np.asarray(m, np.float64).reshape(16).astype(np.float32))
+
+
+def ref_loop_las(cam, cl, box_mins, fr):
+    view, proj, w, h = cam
+    fb = np.full(O.fb_words(w, h), L.DEFAULT_CLEAR, np.uint64)
+    n = cl["n"]
+    lo, md, hi = (O.pad_stream(a, n=n) for a in (cl["lo"], cl["md"], cl["hi"]))
+    b = np.ascontiguousarray(cl["batches"])
+    files = shader_files(fr, box_mins)
+    fv, fp = f32(view), f32(proj)
+    assert O.shaderref().ref_loop_las_render(b.ctypes.data, len(b), lo.ctypes.data, md.ctypes.data,
+                                             hi.ctypes.data, files.ctypes.data, fv.ctypes.data,
+                                             fp.ctypes.data, w, h, 1, n, fb.ctypes.data) == 0
+    return fb
+
+
+def oracle_loop_las(cam, cl, box_mins, mode):
+    with O.arith(mode):
+        fr = oracle_frame(cam, box_mins, O.L0_X12)
+        fb = O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], None,
+                              clear=L.DEFAULT_CLEAR)
+    return fr, fb
+
+
+@pytest.mark.parametrize("camname", ["far", "near", "mid", "corner"])
+def test_loop_las_literal_oracle_is_the_reference_shader(camname):
+    """compute_loop_las/render.cs: 10/20/30-bit decode (H1's X_12 included),
+    culling, precision level, early-z read and atomicMin, index payload."""
+    cl = encoded()
+    cam = cameras(cl)[camname]
+    bm = cl["box_min"][None]
+    fr, want = oracle_loop_las(cam, cl, bm, O.ARITH_LITERAL)
+    got = ref_loop_las(cam, cl, bm, fr)
+    assert (got != L.DEFAULT_CLEAR).sum() > 1000
+    assert np.array_equal(got, want), int(np.argmax(got != want))
+    # the contract (the kernels' arithmetic) differs only by its rounding choices
+    _, contract = oracle_loop_las(cam, cl, bm, O.ARITH_CONTRACT)
+    assert not np.array_equal(contract, want)
+
+
+def test_loop_las_literal_oracle_is_the_reference_shader_many_files():
+    """Per-file records through the shader's ssFiles[batch.fileIndex]."""
+    cl = many_file_cloud(nfiles=24, base=10241, spread=900)
+    for camname, cam in many_file_cameras(cl).items():
+        fr, want = oracle_loop_las(cam, cl, cl["box_min"], O.ARITH_LITERAL)
+        got = ref_loop_las(cam, cl, cl["box_min"], fr)
+        assert np.array_equal(got, want), (camname, int(np.argmax(got != want)))

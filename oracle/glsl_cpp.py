@@ -23,16 +23,18 @@ import sys
 from pathlib import Path
 
 # exact (old, new) replacements per shader, keyed by the path's last two parts
+_BATCHED = [
+    # GLSL converts ivec2 to vec2 implicitly in mixed arithmetic
+    ("uniforms.imageSize.xy * (projCenter.xy", "vec2(uniforms.imageSize) * (projCenter.xy"),
+    ("uniforms.imageSize.xy * (projEdge.xy", "vec2(uniforms.imageSize) * (projEdge.xy"),
+    ("* 0.5f + 0.5f) * uniforms.imageSize;", "* 0.5f + 0.5f) * vec2(uniforms.imageSize);"),
+    # swizzles of temporaries: glm's swizzle members need an lvalue vector
+    ("(file.world * vec4(wgMin, 1.0f)).xyz", "vec3(file.world * vec4(wgMin, 1.0f))"),
+    ("(file.world * vec4(wgMax, 1.0f)).xyz", "vec3(file.world * vec4(wgMax, 1.0f))"),
+]
 FIXUPS = {
-    "compute_loop_las/render.cs": [
-        # GLSL converts ivec2 to vec2 implicitly in mixed arithmetic
-        ("uniforms.imageSize.xy * (projCenter.xy", "vec2(uniforms.imageSize) * (projCenter.xy"),
-        ("uniforms.imageSize.xy * (projEdge.xy", "vec2(uniforms.imageSize) * (projEdge.xy"),
-        ("* 0.5f + 0.5f) * uniforms.imageSize;", "* 0.5f + 0.5f) * vec2(uniforms.imageSize);"),
-        # swizzles of temporaries: glm's swizzle members need an lvalue vector
-        ("(file.world * vec4(wgMin, 1.0f)).xyz", "vec3(file.world * vec4(wgMin, 1.0f))"),
-        ("(file.world * vec4(wgMax, 1.0f)).xyz", "vec3(file.world * vec4(wgMax, 1.0f))"),
-    ],
+    "compute_loop_las/render.cs": _BATCHED,
+    "compute_loop_las2/render.cs": _BATCHED,
 }
 
 

@@ -166,6 +166,8 @@ def shaderref() -> C.CDLL:
     P, I32, I64 = C.c_void_p, C.c_int32, C.c_int64
     g.ref_loop_las_render.argtypes = [P, I64, P, P, P, P, P, P, I32, I32, I32, I64, P]
     g.ref_loop_las_render.restype = C.c_int
+    g.ref_loop_las2_render.argtypes = [P, I64, P, P, P, P, P, P, I32, I32, I32, I64, P]
+    g.ref_loop_las2_render.restype = C.c_int
     return g
 
 

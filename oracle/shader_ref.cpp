@@ -13,6 +13,7 @@
 #include <cstring>
 
 #include "loop_las_render.cpp"
+#include "loop_las2_render.cpp"
 
 extern "C" {
 
@@ -44,6 +45,44 @@ int ref_loop_las_render(const void* batches, int64_t num_batches, const uint32_t
     uniforms.colorizeChunks = false;
     uniforms.colorizeOverdraw = false;
     for (int64_t b = 0; b < num_batches; b++)
+        for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
+            gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
+            gl_LocalInvocationID = uvec3(t, 0u, 0u);
+            gl_GlobalInvocationID = uvec3((uint)b * gl_WorkGroupSize.x + t, 0u, 0u);
+            shader_main();
+        }
+    return 0;
+}
+
+// compute_loop_las2/render.cs dispatched as compute_loop_las2.h:234 does:
+// ceil(numPointsLoaded / 10240) workgroups (-1 if that exceeds the records).
+// The streams are read as uvec4 from firstPoint / 4 up to 10,240 words on, so
+// each must hold the last record's firstPoint + 10,244 words.
+int ref_loop_las2_render(const void* batches, int64_t num_batches, const uint32_t* lo,
+                         const uint32_t* md, const uint32_t* hi, const void* files,
+                         const float view[16], const float proj[16], int32_t width,
+                         int32_t height, int32_t frustum_culling, int64_t num_points,
+                         uint64_t* fb) {
+    using namespace loop_las2;
+    const int64_t dispatch = (num_points + 10239) / 10240;
+    if (dispatch > num_batches) return -1;
+    ssFramebuffer = fb;
+    ssBatches = const_cast<Batch*>(static_cast<const Batch*>(batches));
+    ssXyz_4b = reinterpret_cast<uvec4*>(const_cast<uint32_t*>(lo));
+    ssXyz_8b = reinterpret_cast<uvec4*>(const_cast<uint32_t*>(md));
+    ssXyz_12b = reinterpret_cast<uvec4*>(const_cast<uint32_t*>(hi));
+    ssRGBA = nullptr;
+    ssFiles = const_cast<File*>(static_cast<const File*>(files));
+    std::memset(&debug, 0, sizeof(debug));
+    std::memset(&boundingBoxes, 0, sizeof(boundingBoxes));
+    std::memset(&uniforms, 0, sizeof(uniforms));
+    std::memcpy(&uniforms.view[0][0], view, 16 * sizeof(float));
+    std::memcpy(&uniforms.proj[0][0], proj, 16 * sizeof(float));
+    uniforms.pointsPerThread = 80;  // compute_loop_las2.h:157
+    uniforms.enableFrustumCulling = frustum_culling;
+    uniforms.numPoints = (int)num_points;
+    uniforms.imageSize = ivec2(width, height);
+    for (int64_t b = 0; b < dispatch; b++)
         for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
             gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
             gl_LocalInvocationID = uvec3(t, 0u, 0u);

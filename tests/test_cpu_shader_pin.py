@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from compute_rasterizer_gb300 import _lib as L
-from helpers import cameras, encoded, many_file_cameras, many_file_cloud, oracle_frame
+from helpers import QUIRKS, cameras, encoded, many_file_cameras, many_file_cloud, oracle_frame
 from oracle import oracle as O
 
 pytestmark = pytest.mark.skipif(not O.SHADERREF.exists(),
@@ -81,4 +81,58 @@ def test_loop_las_literal_oracle_is_the_reference_shader_many_files():
     for camname, cam in many_file_cameras(cl).items():
         fr, want = oracle_loop_las(cam, cl, cl["box_min"], O.ARITH_LITERAL)
         got = ref_loop_las(cam, cl, cl["box_min"], fr)
+        assert np.array_equal(got, want), (camname, int(np.argmax(got != want)))
+
+
+def ref_loop_las2(cam, cl, box_mins, fr):
+    """compute_loop_las2/render.cs; its uvec4 prefetch reads up to 10,240 words
+    past a batch's firstPoint / 4 whatever the batch holds, so the streams are
+    padded (with zeros, as the device streams' tails) to cover them."""
+    view, proj, w, h = cam
+    fb = np.full(O.fb_words(w, h), L.DEFAULT_CLEAR, np.uint64)
+    n = cl["n"]
+    words = int(cl["batches"]["first_point"].max()) + 10240 + 64
+    lo, md, hi = (O.pad_stream(a, pad=words - len(a)) for a in (cl["lo"], cl["md"], cl["hi"]))
+    b = np.ascontiguousarray(cl["batches"])
+    files = shader_files(fr, box_mins)
+    fv, fp = f32(view), f32(proj)
+    assert O.shaderref().ref_loop_las2_render(b.ctypes.data, len(b), lo.ctypes.data,
+                                              md.ctypes.data, hi.ctypes.data, files.ctypes.data,
+                                              fv.ctypes.data, fp.ctypes.data, w, h, 1, n,
+                                              fb.ctypes.data) == 0
+    return fb
+
+
+def oracle_loop_las2(cam, cl, box_mins, mode):
+    with O.arith(mode):
+        fr = oracle_frame(cam, box_mins, QUIRKS[L.METHOD_LOOP_LAS_PREFETCH])
+        fb = O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], None,
+                              clear=L.DEFAULT_CLEAR)
+    return fr, fb
+
+
+@pytest.mark.parametrize("camname", ["far", "near", "mid", "corner"])
+def test_loop_las2_literal_oracle_is_the_reference_shader(camname):
+    """compute_loop_las2/render.cs (loop_las_prefetch): the uvec4 prefetch loop,
+    `localIndex > numPoints` (one point past a partial batch, H2), and
+    ceil(numPoints / 10240) workgroups (H3)."""
+    cl = encoded()
+    cam = cameras(cl)[camname]
+    bm = cl["box_min"][None]
+    fr, want = oracle_loop_las2(cam, cl, bm, O.ARITH_LITERAL)
+    got = ref_loop_las2(cam, cl, bm, fr)
+    assert (got != L.DEFAULT_CLEAR).sum() > 1000
+    assert np.array_equal(got, want), int(np.argmax(got != want))
+
+
+def test_loop_las2_uvec4_base_matches_the_reference_shader():
+    """Files whose first points fall on every firstPoint % 4: the shader's
+    uvec4 base firstPoint / 4 + tid drops thread 0 and the batch's last
+    firstPoint % 4 points (H6), which the oracle's CR_QUIRK_UVEC4_BASE rule
+    reproduces."""
+    cl = many_file_cloud(nfiles=24, base=10241, spread=900)
+    assert {int(f) % 4 for f in cl["batches"]["first_point"]} == {0, 1, 2, 3}
+    for camname, cam in many_file_cameras(cl).items():
+        fr, want = oracle_loop_las2(cam, cl, cl["box_min"], O.ARITH_LITERAL)
+        got = ref_loop_las2(cam, cl, cl["box_min"], fr)
         assert np.array_equal(got, want), (camname, int(np.argmax(got != want)))

@@ -35,6 +35,8 @@ _BATCHED = [
 FIXUPS = {
     "compute_loop_las/render.cs": _BATCHED,
     "compute_loop_las2/render.cs": _BATCHED,
+    "compute_loop_las_hqs/depth.cs": _BATCHED[:3],
+    "compute_loop_las_hqs/color.cs": _BATCHED,
 }
 
 

@@ -45,6 +45,29 @@ typedef unsigned int uint;
 
 static uvec3 gl_WorkGroupID(0u), gl_LocalInvocationID(0u), gl_GlobalInvocationID(0u);
 
+// barrier(): the invocations run one after another, so each has finished its
+// previous loop steps when the next starts; the translated shaders share no
+// memory through the barrier (hqs/depth.cs orders nothing with it).
+inline void barrier() {}
+
+// Subgroups of one invocation: a partition holds only the calling
+// invocation, which leads it and owns its sums.  hqs/color.cs adds each
+// partition's integer sums to the accumulators, so any grouping gives the
+// same accumulators.
+static const struct { uint x; } gl_SubgroupInvocationID = {0u};  // GLSL's scalar .x
+template <class T>
+inline uvec4 subgroupPartitionNV(T) {
+    return uvec4(1u, 0u, 0u, 0u);
+}
+template <class T>
+inline T subgroupPartitionedMinNV(T v, uvec4) {
+    return v;
+}
+template <class T>
+inline T subgroupPartitionedAddNV(T v, uvec4) {
+    return v;
+}
+
 template <class T, class U>
 inline T atomicAdd(T& a, U v) {
     const T old = a;

@@ -168,6 +168,8 @@ def shaderref() -> C.CDLL:
     g.ref_loop_las_render.restype = C.c_int
     g.ref_loop_las2_render.argtypes = [P, I64, P, P, P, P, P, P, I32, I32, I32, I64, P]
     g.ref_loop_las2_render.restype = C.c_int
+    g.ref_hqs_render.argtypes = [P, I64, P, P, P, P, P, P, P, I32, I32, I32, I64, P, P]
+    g.ref_hqs_render.restype = C.c_int
     return g
 
 

@@ -14,6 +14,8 @@
 
 #include "loop_las_render.cpp"
 #include "loop_las2_render.cpp"
+#include "hqs_depth.cpp"
+#include "hqs_color.cpp"
 
 extern "C" {
 
@@ -89,6 +91,71 @@ int ref_loop_las2_render(const void* batches, int64_t num_batches, const uint32_
             gl_GlobalInvocationID = uvec3((uint)b * gl_WorkGroupSize.x + t, 0u, 0u);
             shader_main();
         }
+    return 0;
+}
+
+// compute_loop_las_hqs: depth.cs then color.cs, each over ceil(numPoints /
+// 10240) workgroups (compute_loop_las_hqs.h:238, :267; -1 if that exceeds the
+// records).  depth: u32 per pixel; accum: two int64 per pixel (R | G << 32,
+// B | count << 32), as the caller cleared them.
+int ref_hqs_render(const void* batches, int64_t num_batches, const uint32_t* lo, const uint32_t* md,
+                   const uint32_t* hi, const uint32_t* rgba, const void* files, const float view[16],
+                   const float proj[16], int32_t width, int32_t height, int32_t frustum_culling,
+                   int64_t num_points, uint32_t* depth, int64_t* accum) {
+    const int64_t dispatch = (num_points + 10239) / 10240;
+    if (dispatch > num_batches) return -1;
+    {
+        using namespace hqs_depth;
+        ssFbo_depth = depth;
+        ssFbo_rgba = accum;
+        ssBatches = const_cast<Batch*>(static_cast<const Batch*>(batches));
+        ssXyz_4b = const_cast<uint32_t*>(lo);
+        ssXyz_8b = const_cast<uint32_t*>(md);
+        ssXyz_12b = const_cast<uint32_t*>(hi);
+        ssRGBA = const_cast<uint32_t*>(rgba);
+        ssFiles = const_cast<File*>(static_cast<const File*>(files));
+        std::memset(&debug, 0, sizeof(debug));
+        std::memset(&boundingBoxes, 0, sizeof(boundingBoxes));
+        std::memset(&uniforms, 0, sizeof(uniforms));
+        std::memcpy(&uniforms.view[0][0], view, 16 * sizeof(float));
+        std::memcpy(&uniforms.proj[0][0], proj, 16 * sizeof(float));
+        uniforms.pointsPerThread = 80;  // compute_loop_las_hqs.h:162
+        uniforms.enableFrustumCulling = frustum_culling;
+        uniforms.numPoints = (int)num_points;
+        uniforms.imageSize = ivec2(width, height);
+        for (int64_t b = 0; b < dispatch; b++)
+            for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
+                gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
+                gl_LocalInvocationID = uvec3(t, 0u, 0u);
+                shader_main();
+            }
+    }
+    {
+        using namespace hqs_color;
+        ssFbo_depth = depth;
+        ssFbo_rgba = accum;
+        ssBatches = const_cast<Batch*>(static_cast<const Batch*>(batches));
+        ssXyz_4b = const_cast<uint32_t*>(lo);
+        ssXyz_8b = const_cast<uint32_t*>(md);
+        ssXyz_12b = const_cast<uint32_t*>(hi);
+        ssRGBA = const_cast<uint32_t*>(rgba);
+        ssFiles = const_cast<File*>(static_cast<const File*>(files));
+        std::memset(&debug, 0, sizeof(debug));
+        std::memset(&boundingBoxes, 0, sizeof(boundingBoxes));
+        std::memset(&uniforms, 0, sizeof(uniforms));
+        std::memcpy(&uniforms.view[0][0], view, 16 * sizeof(float));
+        std::memcpy(&uniforms.proj[0][0], proj, 16 * sizeof(float));
+        uniforms.pointsPerThread = 80;
+        uniforms.enableFrustumCulling = frustum_culling;
+        uniforms.numPoints = (int)num_points;
+        uniforms.imageSize = ivec2(width, height);
+        for (int64_t b = 0; b < dispatch; b++)
+            for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
+                gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
+                gl_LocalInvocationID = uvec3(t, 0u, 0u);
+                shader_main();
+            }
+    }
     return 0;
 }
 

@@ -136,3 +136,30 @@ def test_loop_las2_uvec4_base_matches_the_reference_shader():
         fr, want = oracle_loop_las2(cam, cl, cl["box_min"], O.ARITH_LITERAL)
         got = ref_loop_las2(cam, cl, cl["box_min"], fr)
         assert np.array_equal(got, want), (camname, int(np.argmax(got != want)))
+
+
+@pytest.mark.parametrize("camname", ["far", "near", "mid", "corner"])
+def test_hqs_literal_oracle_is_the_reference_shaders(camname):
+    """compute_loop_las_hqs/depth.cs then color.cs: the u32 depth pass, the
+    1.01 depth window and the two 64-bit (R | G << 32, B | count << 32)
+    accumulators per pixel."""
+    cl = encoded()
+    view, proj, w, h = cam = cameras(cl)[camname]
+    bm = cl["box_min"][None]
+    with O.arith(O.ARITH_LITERAL):
+        fr = oracle_frame(cam, bm, QUIRKS[L.METHOD_LOOP_LAS_HQS])
+        depth, accum, _ = O.hqs(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+    n = cl["n"]
+    lo, md, hi, rgba = (O.pad_stream(a, n=n) for a in (cl["lo"], cl["md"], cl["hi"], cl["rgba"]))
+    got_d = np.full(O.fb_words(w, h), 0xFF800000, np.uint32)
+    got_a = np.zeros(2 * O.fb_words(w, h), np.int64)
+    b = np.ascontiguousarray(cl["batches"])
+    files = shader_files(fr, bm)
+    fv, fp = f32(view), f32(proj)
+    assert O.shaderref().ref_hqs_render(b.ctypes.data, len(b), lo.ctypes.data, md.ctypes.data,
+                                        hi.ctypes.data, rgba.ctypes.data, files.ctypes.data,
+                                        fv.ctypes.data, fp.ctypes.data, w, h, 1, n,
+                                        got_d.ctypes.data, got_a.ctypes.data) == 0
+    assert (got_d != 0xFF800000).sum() > 1000
+    assert np.array_equal(got_d, depth), int(np.argmax(got_d != depth))
+    assert np.array_equal(got_a.view(np.uint64), accum), int(np.argmax(got_a.view(np.uint64) != accum))

@@ -5,7 +5,7 @@ target; its output goes to oracle/_ref/ only and is never committed).
 usage: glsl_cpp.py SHADER.cs OUT.cpp NAMESPACE
 
 The translation is textual and keeps every statement of the shader as it is:
-  - `#version` / `#extension` lines are dropped;
+  - comments and `#version` / `#extension` lines are dropped;
   - `layout(local_size_x = N) in;` becomes the workgroup-size constant;
   - a buffer block holding one unsized array becomes a pointer of that type,
     a block with members (and a uniform block) a struct plus one instance;
@@ -37,14 +37,34 @@ FIXUPS = {
     "compute_loop_las2/render.cs": _BATCHED,
     "compute_loop_las_hqs/depth.cs": _BATCHED[:3],
     "compute_loop_las_hqs/color.cs": _BATCHED,
+    "compute_loop_las/resolve.cs": [],
+    "compute_loop_las_hqs/resolve.cs": [
+        # x / 0 traps in C++; GLSL leaves it undefined, and the shader
+        # overwrites r, g, b where count is 0
+        ("uint32_t r = R / count;", "uint32_t r = glsl_udiv(R, count);"),
+        ("uint32_t g = G / count;", "uint32_t g = glsl_udiv(G, count);"),
+        ("uint32_t b = B / count;", "uint32_t b = glsl_udiv(B, count);"),
+    ],
+    "compute_2021_earlyz/render.cs": [
+        ("* 0.5f + 0.5f) * uImageSize;", "* 0.5f + 0.5f) * vec2(uImageSize);"),
+    ],
+    "compute_2021_earlyz/resolve.cs": [],
 }
 
 
 def translate(src: str, key: str) -> str:
+    # comments out first (the shaders hold no string literals)
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
     lines = [l for l in src.splitlines() if not re.match(r"\s*#\s*(version|extension)\b", l)]
     s = "\n".join(lines) + "\n"
-    s = re.sub(r"layout\s*\(\s*local_size_x\s*=\s*(\d+)[^)]*\)\s*in\s*;",
-               r"static const uvec3 gl_WorkGroupSize(\1u, 1u, 1u);", s)
+    def wgsize(m):
+        y = re.search(r"local_size_y\s*=\s*(\d+)", m.group(0))
+        return f"static const uvec3 gl_WorkGroupSize({m.group(1)}u, {y.group(1) if y else 1}u, 1u);"
+
+    s = re.sub(r"layout\s*\(\s*local_size_x\s*=\s*(\d+)[^)]*\)\s*in\s*;", wgsize, s)
+    s = re.sub(r"layout\s*\([^)]*\)\s*(?:(?:coherent|readonly|writeonly|restrict)\s+)*uniform\s+uimage2D\s+(\w+)\s*;",
+               r"static uimage2D \1;", s)
     s = re.sub(r"layout\s*\([^)]*\)\s*buffer\s+\w+\s*\{\s*(\w+)\s+(\w+)\s*\[\s*\]\s*;\s*\}\s*;",
                r"static \1* \2 = nullptr;", s)
 
@@ -55,6 +75,10 @@ def translate(src: str, key: str) -> str:
 
     s = re.sub(r"layout\s*\([^)]*\)\s*(?:buffer|uniform)\s+(\w+)\s*\{(.*?)\}\s*(\w+)\s*;", block, s,
                flags=re.S)
+    # a buffer block with one unsized array and no instance name, any layout
+    s = re.sub(r"layout\s*\([^)]*\)\s*buffer\s+\w+\s*\{\s*(\w+)\s+(\w+)\s*\[\s*\]\s*;\s*\}\s*;",
+               r"static \1* \2 = nullptr;", s)
+    s = re.sub(r"layout\s*\([^)]*\)\s*uniform\s+(\w+)\s+(\w+)\s*;", r"static \1 \2;", s)
     s = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void shader_main()", s)
     s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?)(?![\w.])", r"\1f", s)
     s = re.sub(r"\b(\w+)\[(\d+)\]\s+(\w+)\s*\(", r"std::array<\1, \2> \3(", s)

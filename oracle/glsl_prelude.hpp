@@ -68,6 +68,41 @@ inline T subgroupPartitionedAddNV(T v, uvec4) {
     return v;
 }
 
+// A bound image: width x height texels, r32ui (one uint) or rgba8ui (four
+// bytes).  GLSL drops stores outside the image.
+struct uimage2D {
+    void* data;
+    int width, height;
+    int rgba8;
+};
+typedef int sampler2D;  // bound but unread by the translated shaders
+inline ivec2 imageSize(const uimage2D& im) { return ivec2(im.width, im.height); }
+inline bool image_inside(const uimage2D& im, ivec2 p) {
+    return p.x >= 0 && p.y >= 0 && p.x < im.width && p.y < im.height;
+}
+inline void imageStore(uimage2D& im, ivec2 p, uvec4 v) {
+    if (!image_inside(im, p)) return;
+    const size_t i = (size_t)p.y * (size_t)im.width + (size_t)p.x;
+    if (im.rgba8) {
+        uint8_t* t = static_cast<uint8_t*>(im.data) + 4 * i;
+        const uint c[4] = {v.x, v.y, v.z, v.w};
+        for (int k = 0; k < 4; k++) t[k] = (uint8_t)(c[k] < 255u ? c[k] : 255u);  // rgba8ui saturates
+    } else {
+        static_cast<uint*>(im.data)[i] = v.x;
+    }
+}
+inline uint imageAtomicExchange(uimage2D& im, ivec2 p, uint v) {
+    if (!image_inside(im, p) || im.rgba8) return 0u;
+    uint* t = static_cast<uint*>(im.data) + (size_t)p.y * (size_t)im.width + (size_t)p.x;
+    const uint old = *t;
+    *t = v;
+    return old;
+}
+
+// Unsigned division where GLSL leaves x / 0 undefined but does not trap
+// (C++ would); the translated shaders overwrite such results.
+inline uint glsl_udiv(uint a, uint b) { return b ? a / b : 0xFFFFFFFFu; }
+
 template <class T, class U>
 inline T atomicAdd(T& a, U v) {
     const T old = a;

@@ -16,6 +16,28 @@
 #include "loop_las2_render.cpp"
 #include "hqs_depth.cpp"
 #include "hqs_color.cpp"
+#include "las_resolve.cpp"
+#include "hqs_resolve.cpp"
+#include "earlyz_render.cpp"
+#include "earlyz_resolve.cpp"
+
+namespace {
+
+// A groups_x x groups_y dispatch of a 2-D workgroup shader.
+template <class F>
+void dispatch2d(uint groups_x, uint groups_y, uvec3 size, F&& shader_main) {
+    for (uint gy = 0; gy < groups_y; gy++)
+        for (uint gx = 0; gx < groups_x; gx++)
+            for (uint ly = 0; ly < size.y; ly++)
+                for (uint lx = 0; lx < size.x; lx++) {
+                    gl_WorkGroupID = uvec3(gx, gy, 0u);
+                    gl_LocalInvocationID = uvec3(lx, ly, 0u);
+                    gl_GlobalInvocationID = uvec3(gx * size.x + lx, gy * size.y + ly, 0u);
+                    shader_main();
+                }
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -156,6 +178,70 @@ int ref_hqs_render(const void* batches, int64_t num_batches, const uint32_t* lo,
                 shader_main();
             }
     }
+    return 0;
+}
+
+// compute_loop_las/resolve.cs over ceil(W/16) x ceil(H/16) groups
+// (compute_loop_las.h:253-255).  Invocations past the image's right or bottom
+// edge read framebuffer words beyond W*H (the caller pads fb) and store
+// nothing.  image: W*H r32ui texels.
+int ref_loop_las_resolve(uint64_t* fb, const uint32_t* rgba, int32_t width, int32_t height,
+                         uint32_t* image) {
+    using namespace las_resolve;
+    ssFramebuffer = fb;
+    ssRGBA = const_cast<uint32_t*>(rgba);
+    std::memset(&debug, 0, sizeof(debug));
+    std::memset(&uniforms, 0, sizeof(uniforms));
+    uniforms.imageSize = ivec2(width, height);
+    uOutput = uimage2D{image, width, height, 0};
+    dispatch2d((uint)(width + 15) / 16, (uint)(height + 15) / 16, gl_WorkGroupSize, shader_main);
+    return 0;
+}
+
+// compute_loop_las_hqs/resolve.cs over ceil(W/16) x ceil(H/16) groups
+// (compute_loop_las_hqs.h:288-290); accum as 4 uint words per pixel (R, G, B,
+// count: the two int64 accumulators), padded by the caller as fb above.
+int ref_hqs_resolve(const uint32_t* accum, int32_t width, int32_t height, uint32_t* image) {
+    using namespace hqs_resolve;
+    ssRGBA = const_cast<uint32_t*>(accum);
+    std::memset(&debug, 0, sizeof(debug));
+    std::memset(&uniforms, 0, sizeof(uniforms));
+    uniforms.imageSize = ivec2(width, height);
+    uOutput = uimage2D{image, width, height, 0};
+    dispatch2d((uint)(width + 15) / 16, (uint)(height + 15) / 16, gl_WorkGroupSize, shader_main);
+    return 0;
+}
+
+// compute_2021_earlyz/render.cs: ceil(n / 128) groups over 16-byte points
+// (compute_2021_earlyz.h:118-131; n below its 268M-point chunk).  transform:
+// proj * view * world as the host computes it (compute_2021_earlyz.h:108-113).
+// n must be a multiple of 128: the shader reads every invocation's point.
+int ref_earlyz_render(const void* vertices_, int64_t n, const float transform[16], int32_t width,
+                      int32_t height, uint64_t* fb) {
+    using namespace earlyz_render;
+    if (n % 128 != 0) return -1;
+    vertices = const_cast<Vertex*>(static_cast<const Vertex*>(vertices_));
+    ssFramebuffer = fb;
+    std::memcpy(&uTransform[0][0], transform, 16 * sizeof(float));
+    uImageSize = ivec2(width, height);
+    for (int64_t b = 0; b < n / 128; b++)
+        for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
+            gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
+            gl_LocalInvocationID = uvec3(t, 0u, 0u);
+            shader_main();
+        }
+    return 0;
+}
+
+// compute_2021_earlyz/resolve.cs over floor(W/16) x floor(H/16) groups
+// (compute_2021_earlyz.h:162-164): each resolved pixel's RGBA8 and the
+// re-clear of its framebuffer word.  image: W*H rgba8ui texels.
+int ref_earlyz_resolve(uint64_t* fb, int32_t width, int32_t height, uint8_t* image) {
+    using namespace earlyz_resolve;
+    ssFramebuffer = fb;
+    vertices = nullptr;
+    uOutput = uimage2D{image, width, height, 1};
+    dispatch2d((uint)width / 16, (uint)height / 16, gl_WorkGroupSize, shader_main);
     return 0;
 }
 

@@ -163,3 +163,81 @@ def test_hqs_literal_oracle_is_the_reference_shaders(camname):
     assert (got_d != 0xFF800000).sum() > 1000
     assert np.array_equal(got_d, depth), int(np.argmax(got_d != depth))
     assert np.array_equal(got_a.view(np.uint64), accum), int(np.argmax(got_a.view(np.uint64) != accum))
+
+
+def padded(words, width, height, fill, dtype=np.uint64, per_pixel=1):
+    """A copy of a per-pixel buffer long enough for the resolves' partial
+    16 x 16 tiles, which read words past W*H; the extra words hold `fill`."""
+    h16, w16 = -(-height // 16) * 16, -(-width // 16) * 16
+    need = per_pixel * (h16 * width + w16 + 16)
+    out = np.full(max(need, len(words)), fill, dtype)
+    out[:len(words)] = words
+    return out
+
+
+def test_loop_las_resolve_is_the_reference_shader():
+    """compute_loop_las/resolve.cs (window 0) over ceil(W/16) x ceil(H/16)
+    groups at a size that leaves partial tiles: the index payload's color
+    gather, point index 0 and empty pixels to the background."""
+    cl = encoded()
+    cam = cameras(cl, width=331, height=250)["far"]
+    _, fb = oracle_loop_las(cam, cl, cl["box_min"][None], O.ARITH_LITERAL)
+    w, h = cam[2], cam[3]
+    want = O.resolve_index(w, h, fb, cl["rgba"])
+    got = np.zeros(w * h, np.uint32)
+    rgba = O.pad_stream(cl["rgba"], n=cl["n"])
+    fbp = padded(fb, w, h, 0xFFFFFFFFFFFFFFFF)
+    assert O.shaderref().ref_loop_las_resolve(fbp.ctypes.data, rgba.ctypes.data, w, h,
+                                              got.ctypes.data) == 0
+    assert (want != 0x00443322).sum() > 1000
+    assert np.array_equal(got, want), int(np.argmax(got != want))
+
+
+def test_hqs_resolve_is_the_reference_shader():
+    """compute_loop_las_hqs/resolve.cs: integer means of the accumulated
+    colors, empty pixels to the background, partial tiles."""
+    cl = encoded()
+    cam = cameras(cl, width=331, height=250)["far"]
+    with O.arith(O.ARITH_LITERAL):
+        fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[L.METHOD_LOOP_LAS_HQS])
+        _, accum, want = O.hqs(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+    w, h = cam[2], cam[3]
+    got = np.zeros(w * h, np.uint32)
+    acc = padded(accum, w, h, 0, per_pixel=2)
+    assert O.shaderref().ref_hqs_resolve(acc.ctypes.data, w, h, got.ctypes.data) == 0
+    assert (want != 0x00443322).sum() > 1000
+    assert np.array_equal(got, want), int(np.argmax(got != want))
+
+
+@pytest.mark.parametrize("w,h", [(1920, 1080), (333, 250)])
+def test_earlyz_render_and_resolve_are_the_reference_shaders(w, h):
+    """compute_2021_earlyz/render.cs and resolve.cs (config 1's scene): the
+    early-z depth compare and 64-bit atomicMin over 16-byte points, then the
+    floor(W/16) x floor(H/16) resolve with its re-clear.  The render compares
+    depths only, so two points of one pixel at the same depth keep the first
+    in the shader's order and the smaller key in the oracle's (both outcomes
+    of the reference's race on a GPU): such pixels must agree on the depth."""
+    from compute_rasterizer_gb300 import synth
+    n = 128 * 6000
+    v = synth.uniform_vertices_host(3, n, 100.0)
+    view = synth.look_at([150.0, 150.0, 150.0], [50.0, 50.0, 50.0], [0.0, 0.0, 1.0])
+    proj = synth.perspective(60.0, w / h, 0.1, 1000.0)
+    with O.arith(O.ARITH_LITERAL):
+        want_fb, want_img, want_cleared = O.plain(view, proj, w, h, v)
+    T = np.empty(16, np.float32)
+    vd = np.ascontiguousarray(np.asarray(view, np.float64).reshape(16))
+    pd = np.ascontiguousarray(np.asarray(proj, np.float64).reshape(16))
+    O.lib().or_plain_transform(vd.ctypes.data, pd.ctypes.data, T.ctypes.data)
+    fb = np.full(O.fb_words(w, h), 0xFFFFFFFFFFFFFFFF, np.uint64)
+    g = O.shaderref()
+    vv = np.ascontiguousarray(v)
+    assert g.ref_earlyz_render(vv.ctypes.data, n, T.ctypes.data, w, h, fb.ctypes.data) == 0
+    assert (fb != 0xFFFFFFFFFFFFFFFF).sum() > 10000
+    differ = fb != want_fb
+    assert np.array_equal(fb[differ] >> np.uint64(32), want_fb[differ] >> np.uint64(32))
+    assert differ.sum() <= 16, int(differ.sum())
+    fb[differ] = want_fb[differ]  # the same race outcome on both sides for the resolve
+    img = np.zeros(w * h * 4, np.uint8)
+    assert g.ref_earlyz_resolve(fb.ctypes.data, w, h, img.ctypes.data) == 0
+    assert np.array_equal(img.view(np.uint32), want_img), int(np.argmax(img.view(np.uint32) != want_img))
+    assert np.array_equal(fb, want_cleared)

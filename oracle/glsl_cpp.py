@@ -49,6 +49,13 @@ FIXUPS = {
         ("* 0.5f + 0.5f) * uImageSize;", "* 0.5f + 0.5f) * vec2(uImageSize);"),
     ],
     "compute_2021_earlyz/resolve.cs": [],
+    "compute_loop_nodes/render.cs": [
+        ("uniforms.imageSize.xy * (projCenter.xy", "vec2(uniforms.imageSize) * (projCenter.xy"),
+        ("uniforms.imageSize.xy * (projEdge.xy", "vec2(uniforms.imageSize) * (projEdge.xy"),
+        ("* 0.5f + 0.5f) * uniforms.imageSize;", "* 0.5f + 0.5f) * vec2(uniforms.imageSize);"),
+        # GLSL's min(uint, int) converts the literal; C++ needs it unsigned
+        ("loopSize = min(loopSize, 500);", "loopSize = min(loopSize, 500u);"),
+    ],
 }
 
 

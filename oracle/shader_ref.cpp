@@ -20,6 +20,7 @@
 #include "hqs_resolve.cpp"
 #include "earlyz_render.cpp"
 #include "earlyz_resolve.cpp"
+#include "nodes_render.cpp"
 
 namespace {
 
@@ -242,6 +243,45 @@ int ref_earlyz_resolve(uint64_t* fb, int32_t width, int32_t height, uint8_t* ima
     vertices = nullptr;
     uOutput = uimage2D{image, width, height, 1};
     dispatch2d((uint)width / 16, (uint)height / 16, gl_WorkGroupSize, shader_main);
+    return 0;
+}
+
+// compute_loop_nodes/render.cs (its PREFETCHED body) over one workgroup per
+// node (compute_loop_nodes.h:180-181).  world is the identity and view, proj,
+// transform = proj * view * world the float matrices compute_loop_nodes.h:
+// 126-139 uploads; transformFrustum = transform.  The uvec4 reads run up to
+// (min(ceil(n / 128), 500) + 4) / 4 vectors per invocation past a node's
+// pointOffset / 4, so the caller pads the streams.
+int ref_loop_nodes_render(const void* batches, int64_t num_batches, const uint32_t* lo,
+                          const uint32_t* md, const uint32_t* hi, const float view[16],
+                          const float proj[16], const float transform[16], int32_t width,
+                          int32_t height, int32_t frustum_culling, int64_t num_points,
+                          uint64_t* fb) {
+    using namespace nodes_render;
+    ssFramebuffer = fb;
+    ssBatches = const_cast<Batch*>(static_cast<const Batch*>(batches));
+    ssXyz_4b = reinterpret_cast<uvec4*>(const_cast<uint32_t*>(lo));
+    ssXyz_8b = reinterpret_cast<uvec4*>(const_cast<uint32_t*>(md));
+    ssXyz_12b = reinterpret_cast<uvec4*>(const_cast<uint32_t*>(hi));
+    ssRGBA = nullptr;
+    std::memset(&debug, 0, sizeof(debug));
+    std::memset(&boundingBoxes, 0, sizeof(boundingBoxes));
+    std::memset(&uniforms, 0, sizeof(uniforms));
+    uniforms.world = mat4(1.0f);
+    std::memcpy(&uniforms.view[0][0], view, 16 * sizeof(float));
+    std::memcpy(&uniforms.proj[0][0], proj, 16 * sizeof(float));
+    std::memcpy(&uniforms.transform[0][0], transform, 16 * sizeof(float));
+    std::memcpy(&uniforms.transformFrustum[0][0], transform, 16 * sizeof(float));
+    uniforms.pointsPerThread = 80;
+    uniforms.enableFrustumCulling = frustum_culling;
+    uniforms.numPoints = (int)num_points;
+    uniforms.imageSize = ivec2(width, height);
+    for (int64_t b = 0; b < num_batches; b++)
+        for (uint t = 0; t < gl_WorkGroupSize.x; t++) {
+            gl_WorkGroupID = uvec3((uint)b, 0u, 0u);
+            gl_LocalInvocationID = uvec3(t, 0u, 0u);
+            shader_main();
+        }
     return 0;
 }
 

@@ -241,3 +241,49 @@ def test_earlyz_render_and_resolve_are_the_reference_shaders(w, h):
     assert g.ref_earlyz_resolve(fb.ctypes.data, w, h, img.ctypes.data) == 0
     assert np.array_equal(img.view(np.uint32), want_img), int(np.argmax(img.view(np.uint32) != want_img))
     assert np.array_equal(fb, want_cleared)
+
+
+@pytest.fixture(scope="module")
+def octree_nodes(tmp_path_factory):
+    """A Potree 2.0 octree of an 800,000-point terrain, encoded one batch per
+    node (the root over 64,512 points, so the 500-step loop cap cuts it)."""
+    from compute_rasterizer_gb300 import potree, synth
+    from helpers import camera_views, terrain_las
+    d = tmp_path_factory.mktemp("pin_octree")
+    n = 800_000
+    _, rec, hdr = terrain_las(n, 400.0, 3)
+    nodes = potree.write_octree(d, rec, n, hdr.scale[:], hdr.offset[:], hdr.min[:], hdr.max[:],
+                                max_leaf=20000, chunk_levels=2)
+    assert max(nd["num_points"] for nd in nodes) > 64512
+    o = potree.open_octree(d)
+    enc = o.encode()
+    o.close()
+    extent = np.array(hdr.max[:]) - np.array(hdr.min[:])
+    views = camera_views(np.zeros(3), extent, enc[0])
+    proj = synth.perspective(60.0, 400 / 250, 0.1, 200000.0)
+    return enc, n, {k: (v, proj, 400, 250) for k, v in views.items()}
+
+
+@pytest.mark.parametrize("camname", ["far", "mid", "near", "corner"])
+def test_loop_nodes_literal_oracle_is_the_reference_shader(octree_nodes, camname):
+    """compute_loop_nodes/render.cs: one workgroup per node, min(ceil(n/128),
+    500) + 4 steps of one uvec4 per invocation, the 80 px level cut and the
+    one world matrix, float uniforms."""
+    enc, n, cams = octree_nodes
+    view, proj, w, h = cam = cams[camname]
+    with O.arith(O.ARITH_LITERAL):
+        fr = O.make_frame(view, proj, w, h, np.zeros((1, 3)), culling=1,
+                          quirks=O.NODE_LOOP | O.LEVEL4_80PX | O.ONE_WORLD, payload=O.PAYLOAD_INDEX,
+                          lod_skip_level=4, float_uniforms=True)
+        want = O.raster_batched(fr, enc[0], n, *enc[1:4], None, clear=L.DEFAULT_CLEAR)
+    batches = np.ascontiguousarray(enc[0])
+    words = int(batches["first_point"].max()) + 4 * 128 * 130 + 64
+    lo, md, hi = (O.pad_stream(a, pad=words - len(a)) for a in enc[1:4])
+    T = np.ascontiguousarray(np.frombuffer(bytes(fr.files[0].transform), np.float32))
+    fb = np.full(O.fb_words(w, h), L.DEFAULT_CLEAR, np.uint64)
+    assert O.shaderref().ref_loop_nodes_render(batches.ctypes.data, len(batches), lo.ctypes.data,
+                                               md.ctypes.data, hi.ctypes.data, f32(view).ctypes.data,
+                                               f32(proj).ctypes.data, T.ctypes.data, w, h, 1, n,
+                                               fb.ctypes.data) == 0
+    assert (fb != L.DEFAULT_CLEAR).sum() > 100
+    assert np.array_equal(fb, want), int(np.argmax(fb != want))

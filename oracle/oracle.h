@@ -4,12 +4,18 @@
  * the smoke check and the CPU-baseline leg of the benchmark load it as the
  * checker.  The product (compute_rasterizer_gb300) never links or calls it.
  *
- * Parity status: the reference's kernels are GLSL compute shaders and its host
- * loader needs OpenGL/GLFW/ImGui headers, so neither builds here.  The only
- * reference code that builds is the vendored header-only glm used for the view
- * matrices; oracle/Makefile compiles a probe against it (oracle/_ref) and the
- * CPU tests pin this file's matrix setup to it.  Everything downstream of the
- * matrices is pinned by this restatement plus committed golden vectors.
+ * Parity status: the reference's kernels are GLSL compute shaders, which need
+ * an OpenGL context (none exists here), and its host loader needs
+ * OpenGL/GLFW/ImGui headers.  What builds from its sources, by oracle/Makefile
+ * into oracle/_ref: the vendored glm (the CPU tests pin this file's matrix
+ * setup to it), Sort_Frugal's Morton code, the vendored LASzip, and the GLSL
+ * shaders themselves, translated statement by statement to C++ against that
+ * glm (glsl_cpp.py, glsl_prelude.hpp) and run on the CPU (shader_ref.cpp).
+ * In its literal arithmetic mode (or_set_arith) this file equals those
+ * shaders bit for bit (tests/test_cpu_shader_pin.py: loop_las, loop_las2,
+ * HQS depth / color / resolve, the loop_las and early-z resolves, early-z,
+ * loop_nodes); the contract mode below, which the kernels follow, differs
+ * from it only by the FMA and reciprocal choices GLSL leaves to the driver.
  *
  * ARITHMETIC CONTRACT (GLSL leaves division, length() and contraction to the
  * driver; this contract fixes them, and the CUDA kernels follow it bit for bit):

@@ -49,6 +49,12 @@ FIXUPS = {
         ("* 0.5f + 0.5f) * uImageSize;", "* 0.5f + 0.5f) * vec2(uImageSize);"),
     ],
     "compute_2021_earlyz/resolve.cs": [],
+    "compute_2021_dedup/render.cs": [
+        ("* 0.5f + 0.5f) * uImageSize;", "* 0.5f + 0.5f) * vec2(uImageSize);"),
+    ],
+    "compute_2021_earlyz_reduce/render.cs": [
+        ("* 0.5f + 0.5f) * uImageSize;", "* 0.5f + 0.5f) * vec2(uImageSize);"),
+    ],
     "compute_loop_nodes/render.cs": [
         ("uniforms.imageSize.xy * (projCenter.xy", "vec2(uniforms.imageSize) * (projCenter.xy"),
         ("uniforms.imageSize.xy * (projEdge.xy", "vec2(uniforms.imageSize) * (projEdge.xy"),
@@ -86,6 +92,7 @@ def translate(src: str, key: str) -> str:
     s = re.sub(r"layout\s*\([^)]*\)\s*buffer\s+\w+\s*\{\s*(\w+)\s+(\w+)\s*\[\s*\]\s*;\s*\}\s*;",
                r"static \1* \2 = nullptr;", s)
     s = re.sub(r"layout\s*\([^)]*\)\s*uniform\s+(\w+)\s+(\w+)\s*;", r"static \1 \2;", s)
+    s = re.sub(r"(?m)^(\s*)uniform\s+(\w+)\s+(\w+)\s*;", r"\1static \2 \3;", s)
     s = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void shader_main()", s)
     s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?)(?![\w.])", r"\1f", s)
     s = re.sub(r"\b(\w+)\[(\d+)\]\s+(\w+)\s*\(", r"std::array<\1, \2> \3(", s)

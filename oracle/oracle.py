@@ -175,8 +175,10 @@ def shaderref() -> C.CDLL:
     g.ref_earlyz_render.argtypes = [P, I64, P, I32, I32, P]
     g.ref_earlyz_resolve.argtypes = [P, I32, I32, P]
     g.ref_loop_nodes_render.argtypes = [P, I64, P, P, P, P, P, P, I32, I32, I32, I64, P]
+    g.ref_dedup_render.argtypes = [P, I64, P, I32, I32, P]
+    g.ref_reduce_render.argtypes = [P, I64, P, I32, I32, P]
     for k in ("ref_loop_las_resolve", "ref_hqs_resolve", "ref_earlyz_render", "ref_earlyz_resolve",
-              "ref_loop_nodes_render"):
+              "ref_loop_nodes_render", "ref_dedup_render", "ref_reduce_render"):
         getattr(g, k).restype = C.c_int
     return g
 

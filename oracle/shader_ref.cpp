@@ -21,6 +21,8 @@
 #include "earlyz_render.cpp"
 #include "earlyz_resolve.cpp"
 #include "nodes_render.cpp"
+#include "dedup_render.cpp"
+#include "reduce_render.cpp"
 
 namespace {
 
@@ -36,6 +38,23 @@ void dispatch2d(uint groups_x, uint groups_y, uvec3 size, F&& shader_main) {
                     gl_GlobalInvocationID = uvec3(gx * size.x + lx, gy * size.y + ly, 0u);
                     shader_main();
                 }
+}
+
+// A 1D dispatch of `groups` workgroups of 128 invocations in subgroups of 32
+// run in lockstep (glsl_sg::run), the subgroup size of the reference's GPUs.
+void dispatch_subgroups(int64_t groups, void (*shader_main)()) {
+    static glsl_sg::Lockstep ls;
+    uvec3 wg[32], local[32], global[32];
+    for (int64_t b = 0; b < groups; b++)
+        for (uint s = 0; s < 4; s++) {
+            for (uint l = 0; l < 32; l++) {
+                wg[l] = uvec3((uint)b, 0u, 0u);
+                local[l] = uvec3(32u * s + l, 0u, 0u);
+                global[l] = uvec3((uint)b * 128u + 32u * s + l, 0u, 0u);
+            }
+            glsl_sg::run(ls, shader_main, wg, local, global, &gl_WorkGroupID, &gl_LocalInvocationID,
+                         &gl_GlobalInvocationID);
+        }
 }
 
 }  // namespace
@@ -282,6 +301,33 @@ int ref_loop_nodes_render(const void* batches, int64_t num_batches, const uint32
             gl_LocalInvocationID = uvec3(t, 0u, 0u);
             shader_main();
         }
+    return 0;
+}
+
+// compute_2021_dedup/render.cs and compute_2021_earlyz_reduce/render.cs:
+// ceil(n / 128) groups (compute_2021_dedup.h:129-131,
+// compute_2021_earlyz_reduce.h:129-131), subgroups of 32 in lockstep; n a
+// multiple of 128 as for ref_earlyz_render.
+int ref_dedup_render(const void* vertices_, int64_t n, const float transform[16], int32_t width,
+                     int32_t height, uint64_t* fb) {
+    using namespace dedup_render;
+    if (n % 128 != 0) return -1;
+    vertices = const_cast<Vertex*>(static_cast<const Vertex*>(vertices_));
+    ssFramebuffer = fb;
+    std::memcpy(&uTransform[0][0], transform, 16 * sizeof(float));
+    uImageSize = ivec2(width, height);
+    dispatch_subgroups(n / 128, shader_main);
+    return 0;
+}
+int ref_reduce_render(const void* vertices_, int64_t n, const float transform[16], int32_t width,
+                      int32_t height, uint64_t* fb) {
+    using namespace reduce_render;
+    if (n % 128 != 0) return -1;
+    vertices = const_cast<Vertex*>(static_cast<const Vertex*>(vertices_));
+    ssFramebuffer = fb;
+    std::memcpy(&uTransform[0][0], transform, 16 * sizeof(float));
+    uImageSize = ivec2(width, height);
+    dispatch_subgroups(n / 128, shader_main);
     return 0;
 }
 

@@ -287,3 +287,85 @@ def test_loop_nodes_literal_oracle_is_the_reference_shader(octree_nodes, camname
                                                fb.ctypes.data) == 0
     assert (fb != L.DEFAULT_CLEAR).sum() > 100
     assert np.array_equal(fb, want), int(np.argmax(fb != want))
+
+
+@pytest.mark.parametrize("method,variant", [("dedup", 1), ("reduce", 2)])
+@pytest.mark.parametrize("n,w,h", [(128 * 3000, 320, 180), (128 * 1500, 64, 48)])
+def test_warp_variants_are_the_reference_shaders(method, variant, n, w, h):
+    """compute_2021_dedup/render.cs (subgroupPartitionNV + PartitionedMin)
+    and compute_2021_earlyz_reduce/render.cs (subgroupAllEqual, subgroupMin,
+    subgroupClusteredXor / Min over lane pairs, taken only by the lanes the
+    short-circuit reaches) with 32-invocation subgroups in lockstep, against
+    the oracle's warp rules: the random scene and a 64x48 view where most
+    of a subgroup lands on one pixel."""
+    from compute_rasterizer_gb300 import synth
+    v = synth.uniform_vertices_host(3, n, 100.0)
+    view = synth.look_at([150.0, 150.0, 150.0], [50.0, 50.0, 50.0], [0.0, 0.0, 1.0])
+    proj = synth.perspective(60.0, w / h, 0.1, 1000.0)
+    with O.arith(O.ARITH_LITERAL):
+        want, _, _ = O.plain(view, proj, w, h, v, variant=variant)
+    T = np.empty(16, np.float32)
+    vd = np.ascontiguousarray(np.asarray(view, np.float64).reshape(16))
+    pd = np.ascontiguousarray(np.asarray(proj, np.float64).reshape(16))
+    O.lib().or_plain_transform(vd.ctypes.data, pd.ctypes.data, T.ctypes.data)
+    fb = np.full(O.fb_words(w, h), 0xFFFFFFFFFFFFFFFF, np.uint64)
+    vv = np.ascontiguousarray(v)
+    fn = O.shaderref().ref_dedup_render if variant == 1 else O.shaderref().ref_reduce_render
+    assert fn(vv.ctypes.data, n, T.ctypes.data, w, h, fb.ctypes.data) == 0
+    assert (fb != 0xFFFFFFFFFFFFFFFF).sum() > 100
+    assert np.array_equal(fb, want), int(np.argmax(fb != want))
+
+
+def ray_vertices(w, h, rays, seed, pairs):
+    """Points on view rays of pixel centres (view = identity): every subgroup
+    of 32 consecutive points on one ray (pairs=False) or each lane pair on
+    its own ray (pairs=True), depths 2 + k * 2^-20 a few ulps apart along a
+    ray (k the lane, or 0 and 3 within a pair), so that
+    depth << 24 | color lets a farther point's color byte win: which lanes a
+    subgroup lets through decides the framebuffer."""
+    from compute_rasterizer_gb300 import synth
+    proj = np.asarray(synth.perspective(60.0, w / h, 0.1, 1000.0), np.float64).reshape(16)
+    rng = np.random.default_rng(seed)
+    n = 32 * rays
+    lane = np.arange(n) % 32
+    ray = np.arange(n) // (2 if pairs else 32)
+    px, py = rng.integers(0, w, ray.max() + 1)[ray], rng.integers(0, h, ray.max() + 1)[ray]
+    sx, sy = (2.0 * (px + 0.5) / w - 1.0), (2.0 * (py + 0.5) / h - 1.0)
+    depth = 2.0 + ((lane & 1) * 3 if pairs else lane) * 2.0 ** -20
+    v = np.zeros(n, dtype=L.VERTEX_DTYPE)
+    v["x"], v["y"], v["z"] = sx * depth / proj[0], sy * depth / proj[5], -depth
+    v["color"] = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    return v, np.eye(4), proj
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("pairs", [False, True])
+def test_warp_variants_on_crowded_subgroups(variant, pairs):
+    """Subgroups whose lanes share pixels at nearly equal depths: the
+    partitions (dedup), the all-equal fast path and the lane-pair clusters
+    (early-z & reduce) decide which keys reach the framebuffer, and the
+    result differs from every point submitting."""
+    w, h = 64, 48
+    v, view, proj = ray_vertices(w, h, 600, 5 + variant, pairs)
+    n = len(v)
+    with O.arith(O.ARITH_LITERAL):
+        want, _, _ = O.plain(view, proj, w, h, v, variant=variant)
+    T = np.empty(16, np.float32)
+    vd, pd = np.ascontiguousarray(view.reshape(16)), np.ascontiguousarray(proj)
+    O.lib().or_plain_transform(vd.ctypes.data, pd.ctypes.data, T.ctypes.data)
+    fb = np.full(O.fb_words(w, h), 0xFFFFFFFFFFFFFFFF, np.uint64)
+    vv = np.ascontiguousarray(v)
+    fn = O.shaderref().ref_dedup_render if variant == 1 else O.shaderref().ref_reduce_render
+    assert fn(vv.ctypes.data, n, T.ctypes.data, w, h, fb.ctypes.data) == 0
+    assert np.array_equal(fb, want), int(np.argmax(fb != want))
+    # every point submitting its key: the same points one per subgroup (the
+    # other 31 invocations behind the camera, culled) -- the subgroup rules
+    # are what makes the two framebuffers differ
+    spread = np.zeros(32 * n, dtype=L.VERTEX_DTYPE)
+    spread["z"] = 1.0
+    spread[::32] = v
+    with O.arith(O.ARITH_LITERAL):
+        everyone, _, _ = O.plain(view, proj, w, h, spread, variant=variant)
+    assert (want != 0xFFFFFFFFFFFFFFFF).sum() > 300
+    assert np.array_equal(want != 0xFFFFFFFFFFFFFFFF, everyone != 0xFFFFFFFFFFFFFFFF)
+    assert (want != everyone).sum() > 50

@@ -14,8 +14,9 @@
  * In its literal arithmetic mode (or_set_arith) this file equals those
  * shaders bit for bit (tests/test_cpu_shader_pin.py: loop_las, loop_las2,
  * HQS depth / color / resolve, the loop_las and early-z resolves, early-z,
- * the dedup and early-z & reduce warp variants, loop_nodes); the contract mode below, which the kernels follow, differs
- * from it only by the FMA and reciprocal choices GLSL leaves to the driver.
+ * the dedup and early-z & reduce warp variants, loop_nodes); the contract
+ * mode below, which the kernels follow, differs from it only by the FMA and
+ * reciprocal choices GLSL leaves to the driver.
  *
  * ARITHMETIC CONTRACT (GLSL leaves division, length() and contraction to the
  * driver; this contract fixes them, and the CUDA kernels follow it bit for bit):

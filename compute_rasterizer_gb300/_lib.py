@@ -26,6 +26,7 @@ PAYLOAD_INDEX, PAYLOAD_COLOR = 0, 1
 QUIRK_L0_X12, QUIRK_INCLUSIVE_END, QUIRK_DISPATCH_BY_POINTS, QUIRK_UVEC4_BASE, QUIRK_RESOLVE_TILES = \
     1, 2, 4, 8, 16
 QUIRK_NODE_LOOP, QUIRK_LEVEL4_80PX, QUIRK_ONE_WORLD, QUIRK_FLOAT_UNIFORMS = 32, 64, 128, 256
+QUIRK_LITERAL_ARITH = 512
 POTREE_QUIRK_12B_FROM_8B, POTREE_QUIRK_WRAP30, POTREE_QUIRKS_DEFAULT = 1, 2, -1
 MAX_FILES = 65536
 NOALLOC_MAX_BATCHES, NOALLOC_MAX_FILES, NOALLOC_SCRATCH_BYTES = 131064, 1024, 753664

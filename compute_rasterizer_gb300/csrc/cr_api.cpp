@@ -115,11 +115,13 @@ cr_status build_view_params(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* v
     vp->culling = culling ? 1 : 0;
     vp->level4_px = (quirks & CR_QUIRK_LEVEL4_80PX) ? 80.0f : 100.0f;
     vp->one_world = (quirks & CR_QUIRK_ONE_WORLD) ? 1 : 0;
+    const bool literal = (quirks & CR_QUIRK_LITERAL_ARITH) != 0;
+    vp->literal = literal ? 1 : 0;
     for (int f = 0; f < std::min(cloud->nfiles, kInlineFiles); f++) {
         if (quirks & CR_QUIRK_FLOAT_UNIFORMS)
-            file_record_float(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f]);
+            file_record_float(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f], literal);
         else
-            file_record(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f]);
+            file_record(view->view, view->proj, &cloud->box_min[3 * f], &vp->files[f], literal);
     }
     return CR_OK;
 }
@@ -141,7 +143,8 @@ cr_status enqueue_file_records(cr_ctx* ctx, const cr_cloud* cloud, const cr_view
         ctx->files_cap = cloud->nfiles;
     }
     if (launch_file_records(view->view, view->proj, cloud->box_min.data(), cloud->nfiles, ctx->files,
-                            stream, (quirks & CR_QUIRK_FLOAT_UNIFORMS) ? 1 : 0) != 0)
+                            stream, (quirks & CR_QUIRK_FLOAT_UNIFORMS) ? 1 : 0,
+                            (quirks & CR_QUIRK_LITERAL_ARITH) ? 1 : 0) != 0)
         return fail(ctx, CR_ERR_CUDA, "file record launch failed%s", "");
     vp->dfiles = ctx->files;
     return CR_OK;
@@ -243,7 +246,7 @@ int cr::default_quirks_for(int32_t method) { return default_quirks(method); }
 int cr::ctx_device(const cr_ctx* ctx) { return ctx ? ctx->device : 0; }
 
 cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
-                              int32_t culling, ViewParams* vp) {
+                              int32_t culling, ViewParams* vp, int literal) {
     if (!view || !box_min || !vp || num_files < 1 || num_files > kMaxFiles)
         return CR_ERR_INVALID_ARG;
     if (!finite_all(view->view, 16) || !finite_all(view->proj, 16) ||
@@ -256,8 +259,9 @@ cr_status cr::view_params_for(const cr_view* view, const double* box_min, int32_
     vp->nfiles = num_files;
     vp->culling = culling ? 1 : 0;
     vp->level4_px = 100.0f;
+    vp->literal = literal ? 1 : 0;
     for (int f = 0; f < std::min(num_files, kInlineFiles); f++)
-        file_record(view->view, view->proj, &box_min[3 * f], &vp->files[f]);
+        file_record(view->view, view->proj, &box_min[3 * f], &vp->files[f], literal != 0);
     return CR_OK;
 }
 
@@ -808,7 +812,7 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
         const int grid = ctx->num_sms * 8;
         const int variant = p->method == CR_METHOD_DEDUP ? 1 : (p->method == CR_METHOD_EARLYZ_REDUCE ? 2 : 0);
         if (launch_plain(T, fb->W, fb->H, cloud->verts, loaded_points(cloud), fb->fb, grid, variant,
-                         stream) != 0)
+                         stream, (quirks & CR_QUIRK_LITERAL_ARITH) ? 1 : 0) != 0)
             return fail(ctx, CR_ERR_CUDA, "plain raster launch failed%s", "");
         mark(2, CR_STAGE_RASTER);
         mark(3, -1);
@@ -875,7 +879,8 @@ cr_status cr_render(cr_ctx* ctx, const cr_cloud* cloud, const cr_view* view,
         bl.mode = modes[pass];
         int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm
                                          : batched_blocks_per_sm(bl.mode, bl.payload, block,
-                                                                 cloud->nfiles > kInlineFiles);
+                                                                 cloud->nfiles > kInlineFiles,
+                                                                 (quirks & CR_QUIRK_LITERAL_ARITH) != 0);
         if (per_sm < 1) per_sm = 1;
         const int grid = ctx->num_sms * per_sm;
         if (launch_batched(vp, bl, block, grid, stream) != 0)

@@ -126,9 +126,15 @@ __device__ bool intersects_frustum(const float* pl, float mnx, float mny, float 
     return true;
 }
 
-__device__ void mat4_vec4(const float* m, const float v[4], float o[4]) {
+// literal (CR_QUIRK_LITERAL_ARITH): glm's association, (m0 x + m1 y) + (m2 z + m3 w)
+__device__ void mat4_vec4(const float* m, const float v[4], float o[4], bool literal = false) {
 #pragma unroll
     for (int r = 0; r < 4; r++) {
+        if (literal) {
+            o[r] = fadd(fadd(fmul(m[r], v[0]), fmul(m[4 + r], v[1])),
+                        fadd(fmul(m[8 + r], v[2]), fmul(m[12 + r], v[3])));
+            continue;
+        }
         float s = fmul(m[r], v[0]);
         s = fadd(s, fmul(m[4 + r], v[1]));
         s = fadd(s, fmul(m[8 + r], v[2]));
@@ -141,23 +147,30 @@ __device__ void mat4_vec4(const float* m, const float v[4], float o[4]) {
 // compute_loop_nodes/render.cs:199 80)
 __device__ int precision_level(const float* P, const float* VW, int32_t W, int32_t H, float mnx,
                                float mny, float mnz, float mxx, float mxy, float mxz,
-                               float lvl4_px = 100.0f) {
+                               float lvl4_px = 100.0f, bool literal = false) {
     float c[4] = {__fdiv_rn(fadd(mnx, mxx), 2.0f), __fdiv_rn(fadd(mny, mxy), 2.0f),
                   __fdiv_rn(fadd(mnz, mxz), 2.0f), 1.0f};
     float dx = fsub(mnx, mxx), dy = fsub(mny, mxy), dz = fsub(mnz, mxz);
     float radius = __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
     float vc[4], ve[4], pc[4], pe[4];
-    mat4_vec4(VW, c, vc);
+    mat4_vec4(VW, c, vc, literal);
     ve[0] = fadd(vc[0], radius);
     ve[1] = fadd(vc[1], 0.0f);
     ve[2] = fadd(vc[2], 0.0f);
     ve[3] = fadd(vc[3], 0.0f);
-    mat4_vec4(P, vc, pc);
-    mat4_vec4(P, ve, pe);
+    mat4_vec4(P, vc, pc, literal);
+    mat4_vec4(P, ve, pe, literal);
     // render.cs:210-211 `xy / w`: one correctly rounded reciprocal per vector
-    const float rc = rcp_rn(pc[3]), re = rcp_rn(pe[3]);
-    float pcx = fmul(pc[0], rc), pcy = fmul(pc[1], rc);
-    float pex = fmul(pe[0], re), pey = fmul(pe[1], re);
+    // (literal: a division per component)
+    float pcx, pcy, pex, pey;
+    if (literal) {
+        pcx = __fdiv_rn(pc[0], pc[3]); pcy = __fdiv_rn(pc[1], pc[3]);
+        pex = __fdiv_rn(pe[0], pe[3]); pey = __fdiv_rn(pe[1], pe[3]);
+    } else {
+        const float rc = rcp_rn(pc[3]), re = rcp_rn(pe[3]);
+        pcx = fmul(pc[0], rc); pcy = fmul(pc[1], rc);
+        pex = fmul(pe[0], re); pey = fmul(pe[1], re);
+    }
     float Wf = (float)W, Hf = (float)H;
     float scx = __fdiv_rn(fmul(Wf, fadd(pcx, 1.0f)), 2.0f);
     float scy = __fdiv_rn(fmul(Hf, fadd(pcy, 1.0f)), 2.0f);
@@ -243,9 +256,18 @@ __device__ __forceinline__ bool zcache_rejects(const unsigned long long* zc, uin
     return (uint32_t)e == tag && wbits > (uint32_t)(e >> 32);
 }
 
-// Clip-space position of a decoded point (render.cs:399-401).
+// Clip-space position of a decoded point (render.cs:399-401).  LIT
+// (CR_QUIRK_LITERAL_ARITH): `transform * vec4(p, 1.0)` with glm's
+// association, (T0 x + T4 y) + (T8 z + T12 * 1), each operation rounded.
+template <bool LIT = false>
 __device__ __forceinline__ void project_clip(const BatchCtx& c, float x, float y, float z,
                                              float& px, float& py, float& pw) {
+    if (LIT) {
+        px = fadd(fadd(fmul(c.T0, x), fmul(c.T4, y)), fadd(fmul(c.T8, z), fmul(c.T12, 1.0f)));
+        py = fadd(fadd(fmul(c.T1, x), fmul(c.T5, y)), fadd(fmul(c.T9, z), fmul(c.T13, 1.0f)));
+        pw = fadd(fadd(fmul(c.T3, x), fmul(c.T7, y)), fadd(fmul(c.T11, z), fmul(c.T15, 1.0f)));
+        return;
+    }
     px = __fmaf_rn(c.T8, z, __fmaf_rn(c.T4, y, __fmaf_rn(c.T0, x, c.T12)));
     py = __fmaf_rn(c.T9, z, __fmaf_rn(c.T5, y, __fmaf_rn(c.T1, x, c.T13)));
     pw = __fmaf_rn(c.T11, z, __fmaf_rn(c.T7, y, __fmaf_rn(c.T3, x, c.T15)));
@@ -254,16 +276,26 @@ __device__ __forceinline__ void project_clip(const BatchCtx& c, float x, float y
 // Divide, inside test and pixel (render.cs:402-409).  SAFE: the caller
 // guarantees w in [2^-120, 2^120] (w_safe), so the reciprocal needs no range
 // test.
-template <bool SAFE = false>
+template <bool SAFE = false, bool LIT = false>
 __device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, float py, float pw,
                                                int32_t& pix, uint32_t& wbits) {
     // render.cs:402 `pos.xyz / pos.w`: one correctly rounded reciprocal of w
-    const float rw = SAFE ? rcp_rn_normal(pw) : rcp_rn(pw);
-    float qx = fmul(px, rw), qy = fmul(py, rw);
+    // (LIT: a division per component)
+    float qx, qy;
+    if (LIT) {
+        qx = __fdiv_rn(px, pw);
+        qy = __fdiv_rn(py, pw);
+    } else {
+        const float rw = SAFE ? rcp_rn_normal(pw) : rcp_rn(pw);
+        qx = fmul(px, rw);
+        qy = fmul(py, rw);
+    }
     // render.cs:404 written positively, so a NaN position is outside (the
     // negated form would keep it and index the framebuffer with garbage); in
     // w-safe batches w >= 2^-120 at every point, so w > 0 needs no test
     bool in = (SAFE || pw > 0.0f) && qx >= -1.0f && qx <= 1.0f && qy >= -1.0f && qy <= 1.0f;
+    // qx * 0.5 is exact (or, below 2^-125, far under half an ulp of 0.5), so
+    // the fused form rounds as render.cs:406's product then sum does
     int32_t ix = small_f2i(fmul(__fmaf_rn(qx, 0.5f, 0.5f), c.Wf));
     int32_t iy = small_f2i(fmul(__fmaf_rn(qy, 0.5f, 0.5f), c.Hf));
     pix = ix + iy * c.W;
@@ -271,13 +303,14 @@ __device__ __forceinline__ bool project_finish(const BatchCtx& c, float px, floa
     return in;
 }
 
-// Project a decoded point (render.cs:399-409 under the arithmetic contract).
-template <bool SAFE = false>
+// Project a decoded point (render.cs:399-409 under the arithmetic contract,
+// or as written with LIT).
+template <bool SAFE = false, bool LIT = false>
 __device__ __forceinline__ bool project(const BatchCtx& c, float x, float y, float z, int32_t& pix,
                                         uint32_t& wbits) {
     float px, py, pw;
-    project_clip(c, x, y, z, px, py, pw);
-    return project_finish<SAFE>(c, px, py, pw, pix, wbits);
+    project_clip<LIT>(c, x, y, z, px, py, pw);
+    return project_finish<SAFE, LIT>(c, px, py, pw, pix, wbits);
 }
 
 // ---- packed fp32 pairs ------------------------------------------------------

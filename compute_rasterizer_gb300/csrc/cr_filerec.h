@@ -33,7 +33,9 @@ __host__ __device__ inline void mat_mul(const T* a, const T* b, T* out) {
 }
 
 // render.cs:134-174: planes from the rows of transformFrustum, normalised.
-__host__ __device__ inline void frustum_planes(const float* m, float* planes) {
+// literal (CR_QUIRK_LITERAL_ARITH): `vec3(x, y, z) / nLength` divides each
+// component instead of multiplying by one reciprocal.
+__host__ __device__ inline void frustum_planes(const float* m, float* planes, bool literal = false) {
     const float comb[6][4] = {
         {m[3] - m[0], m[7] - m[4], m[11] - m[8], m[15] - m[12]},
         {m[3] + m[0], m[7] + m[4], m[11] + m[8], m[15] + m[12]},
@@ -46,10 +48,16 @@ __host__ __device__ inline void frustum_planes(const float* m, float* planes) {
         const float* p = comb[i];
         const float len = sqrtf((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
         // render.cs:139-140: vec3 / length is one reciprocal, w / length a division
-        const float inv = 1.0f / len;
-        planes[4 * i + 0] = p[0] * inv;
-        planes[4 * i + 1] = p[1] * inv;
-        planes[4 * i + 2] = p[2] * inv;
+        if (literal) {
+            planes[4 * i + 0] = p[0] / len;
+            planes[4 * i + 1] = p[1] / len;
+            planes[4 * i + 2] = p[2] / len;
+        } else {
+            const float inv = 1.0f / len;
+            planes[4 * i + 0] = p[0] * inv;
+            planes[4 * i + 1] = p[1] * inv;
+            planes[4 * i + 2] = p[2] * inv;
+        }
         planes[4 * i + 3] = p[3] / len;
     }
 }
@@ -57,7 +65,7 @@ __host__ __device__ inline void frustum_planes(const float* m, float* planes) {
 // compute_loop_las.h:166-200 for one file: transform = mat4(proj * view *
 // translate(boxMin)) in double, then the float planes and view * world.
 __host__ __device__ inline void file_record(const double* view, const double* proj,
-                                            const double* box_min, FileRec* out) {
+                                            const double* box_min, FileRec* out, bool literal = false) {
     const double world[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0,
                               box_min[0], box_min[1], box_min[2], 1};
     double pv[16], t[16];
@@ -69,7 +77,7 @@ __host__ __device__ inline void file_record(const double* view, const double* pr
         fview[i] = (float)view[i];
         fworld[i] = (float)world[i];
     }
-    frustum_planes(out->T, out->planes);
+    frustum_planes(out->T, out->planes, literal);
     mat_mul(fview, fworld, out->VW);
 }
 
@@ -77,7 +85,8 @@ __host__ __device__ inline void file_record(const double* view, const double* pr
 // transform = (float(proj) * float(view)) * float(world), view * world in
 // float (CR_QUIRK_FLOAT_UNIFORMS).
 __host__ __device__ inline void file_record_float(const double* view, const double* proj,
-                                                  const double* box_min, FileRec* out) {
+                                                  const double* box_min, FileRec* out,
+                                                  bool literal = false) {
     const double world[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0,
                               box_min[0], box_min[1], box_min[2], 1};
     float fv[16], fp[16], fw[16], pv[16];
@@ -88,7 +97,7 @@ __host__ __device__ inline void file_record_float(const double* view, const doub
     }
     mat_mul(fp, fv, pv);
     mat_mul(pv, fw, out->T);
-    frustum_planes(out->T, out->planes);
+    frustum_planes(out->T, out->planes, literal);
     mat_mul(fv, fw, out->VW);
 }
 

@@ -92,6 +92,7 @@ struct ViewParams {
     const FileRec* dfiles;   // nfiles records when nfiles > kInlineFiles, else null
     float level4_px;         // level 4 below this projected size (100; loop_nodes 80)
     int32_t one_world;       // every batch uses file 0's record (CR_QUIRK_ONE_WORLD)
+    int32_t literal;         // CR_QUIRK_LITERAL_ARITH: the precision level as written
 };
 
 // Scratch words at the head of the ctx scratch buffer.  The cull kernel sorts
@@ -135,17 +136,20 @@ struct BatchedLaunch {
 // matrices and the files' boxMin (host array, passed to the kernels in their
 // parameters, 1024 files per launch) into out[0, nfiles).
 int launch_file_records(const double view[16], const double proj[16], const double* box_min,
-                        int32_t nfiles, FileRec* out, void* stream, int float_uniforms = 0);
+                        int32_t nfiles, FileRec* out, void* stream, int float_uniforms = 0,
+                        int literal = 0);
 // list_cap: words of the item-list region (nb_dispatch, or nb_dispatch *
 // kMaxNodeSlices with node_slices).
 int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb_dispatch,
                 int64_t capacity, int32_t quirks, uint32_t* scratch, void* stream,
                 int64_t list_cap = -1, int node_slices = 0);
+// bl.quirks & CR_QUIRK_LITERAL_ARITH selects the literal instances (128 threads)
 int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
                    void* stream);
-// variant 0: early-z, 1: dedup, 2: early-z & reduce (the three plain methods)
+// variant 0: early-z, 1: dedup, 2: early-z & reduce (the three plain methods);
+// literal: CR_QUIRK_LITERAL_ARITH
 int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
-                 uint64_t* fb, int grid, int variant, void* stream);
+                 uint64_t* fb, int grid, int variant, void* stream, int literal = 0);
 // tiles: CR_QUIRK_RESOLVE_TILES (image words outside full 16x16 tiles kept)
 int launch_resolve_index(int32_t W, int32_t H, uint64_t* fb, const uint32_t* rgba,
                          int64_t rgba_words, uint32_t* image, int clear_after, uint64_t clear,
@@ -164,13 +168,13 @@ int launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, void* stream);
 // mismatching bit pattern into *first (synchronous, default stream).
 int launch_check_reciprocal(uint64_t* bad, uint32_t* first);
 // many: the cloud has more than kInlineFiles files (its own kernel instances)
-int batched_blocks_per_sm(int mode, int payload, int block, bool many = false);
+int batched_blocks_per_sm(int mode, int payload, int block, bool many = false, bool literal = false);
 
 // Per-view uniforms from double matrices and per-file boxMin (cr_api.cpp):
 // the records of the first min(num_files, kInlineFiles) files; dfiles is left
 // null and must be set by the caller when num_files > kInlineFiles.
 cr_status view_params_for(const cr_view* view, const double* box_min, int32_t num_files,
-                          int32_t culling, ViewParams* out);
+                          int32_t culling, ViewParams* out, int literal = 0);
 
 // Read-only view of a LAS-derived cloud's device layout (cr_api.cpp).
 struct CloudInfo {

@@ -45,7 +45,7 @@ namespace {
 constexpr int kFilesPerLaunch = 1024;
 struct FileChunk {
     double view[16], proj[16];
-    int32_t first, count, float_uniforms;
+    int32_t first, count, float_uniforms, literal;
     double box_min[3 * kFilesPerLaunch];
 };
 static_assert(sizeof(FileChunk) < 32000, "kernel parameters are limited to 32 KB");
@@ -55,8 +55,8 @@ __global__ void __launch_bounds__(128) k_file_records(const __grid_constant__ Fi
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.count) return;
     FileRec r;
-    if (c.float_uniforms) file_record_float(c.view, c.proj, &c.box_min[3 * i], &r);
-    else file_record(c.view, c.proj, &c.box_min[3 * i], &r);
+    if (c.float_uniforms) file_record_float(c.view, c.proj, &c.box_min[3 * i], &r, c.literal != 0);
+    else file_record(c.view, c.proj, &c.box_min[3 * i], &r, c.literal != 0);
     out[c.first + i] = r;
 }
 
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
             bool vis = !vp.culling || intersects_frustum(f.planes, mnx, mny, mnz, mxx, mxy, mxz);
             if (vis) {
                 int level = precision_level(vp.P, f.VW, vp.W, vp.H, mnx, mny, mnz, mxx, mxy, mxz,
-                                            vp.level4_px);
+                                            vp.level4_px, vp.literal != 0);
                 // compute_loop_nodes/render.cs:273-276: the level-of-detail cut
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
@@ -227,16 +227,23 @@ __device__ __forceinline__ void hqs_color_flush(const BatchedLaunch& bl, bool ac
     }
 }
 
+// float(X) * step + min: one FMA, or (LIT, CR_QUIRK_LITERAL_ARITH) the
+// product then the sum as render.cs:355-357 writes it.
+template <bool LIT>
+__device__ __forceinline__ float decode_axis(float X, float step, float mn) {
+    return LIT ? fadd(fmul(X, step), mn) : __fmaf_rn(X, step, mn);
+}
+
 // Decodes point j of the lane's vector at level class LC (render.cs:333-397).
-template <int LC>
+template <int LC, bool LIT = false>
 __device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, const uint4& w12, int j,
                                              const BatchCtx& c, bool l0_x12, float& x, float& y,
                                              float& z) {
     const uint32_t a = u4get(w4, j);
     if (LC == 2) {
-        x = __fmaf_rn(small_u2f(a & 1023u), c.sx, c.mnx);
-        y = __fmaf_rn(small_u2f((a >> 10) & 1023u), c.sy, c.mny);
-        z = __fmaf_rn(small_u2f((a >> 20) & 1023u), c.sz, c.mnz);
+        x = decode_axis<LIT>(small_u2f(a & 1023u), c.sx, c.mnx);
+        y = decode_axis<LIT>(small_u2f((a >> 10) & 1023u), c.sy, c.mny);
+        z = decode_axis<LIT>(small_u2f((a >> 20) & 1023u), c.sz, c.mnz);
     } else {
         const uint32_t b = u4get(w8, j);
         uint32_t X = ((a & 1023u) << 20) | ((b & 1023u) << 10);
@@ -248,9 +255,9 @@ __device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, c
             if (l0_x12) { y12 = x12; z12 = x12; }
             X |= x12; Y |= y12; Z |= z12;
         }
-        x = __fmaf_rn(__uint2float_rn(X), c.sx, c.mnx);
-        y = __fmaf_rn(__uint2float_rn(Y), c.sy, c.mny);
-        z = __fmaf_rn(__uint2float_rn(Z), c.sz, c.mnz);
+        x = decode_axis<LIT>(__uint2float_rn(X), c.sx, c.mnx);
+        y = decode_axis<LIT>(__uint2float_rn(Y), c.sy, c.mny);
+        z = decode_axis<LIT>(__uint2float_rn(Z), c.sz, c.mnz);
     }
 }
 
@@ -260,7 +267,8 @@ __device__ __forceinline__ void decode_point(const uint4& w4, const uint4& w8, c
 // next vector is loaded before the current one is processed.  PAIRS (full
 // 10-bit batches that the cull flagged w-safe): points are decoded and
 // projected two at a time with the unchecked reciprocal (project_pair10).
-template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false, bool PAIRS = false>
+template <int MODE, int PAYLOAD, int BLOCK, int LC, bool FULL = false, bool PAIRS = false,
+          bool LIT = false>
 __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned long long* zc,
                                            const BatchCtx& c, const PairParams& pp, int64_t first,
                                            int32_t count, bool l0_x12) {
@@ -324,8 +332,8 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
                 for (int j = 0; j < 4; j++) {
                     const bool valid = FULL || ((uint32_t)(rel0 + j) < (uint32_t)count && lane_live);
                     float x, y, z;
-                    decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
-                    ok[j] = project(c, x, y, z, pix[j], wb[j]) && valid;
+                    decode_point<LC, LIT>(w4, w8, w12, j, c, l0_x12, x, y, z);
+                    ok[j] = project<false, LIT>(c, x, y, z, pix[j], wb[j]) && valid;
                 }
             }
             bool cont[4];
@@ -379,10 +387,10 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
                 const bool valid = FULL || ((uint32_t)(rel0 + j) < (uint32_t)count && lane_live);
                 const uint32_t idx = index0 + 4u * (uint32_t)v + (uint32_t)j;
                 float x, y, z;
-                decode_point<LC>(w4, w8, w12, j, c, l0_x12, x, y, z);
+                decode_point<LC, LIT>(w4, w8, w12, j, c, l0_x12, x, y, z);
                 int32_t pix;
                 uint32_t wbits;
-                const bool ok = project(c, x, y, z, pix, wbits) && valid;
+                const bool ok = project<false, LIT>(c, x, y, z, pix, wbits) && valid;
                 const uint32_t color = kNeedColor ? u4get(col, j) : 0u;
                 const uint32_t payload = (PAYLOAD == CR_PAYLOAD_COLOR) ? color : (uint32_t)idx;
                 Emit<MODE>::run(bl, zc, ok, pix, wbits, payload, color);
@@ -405,7 +413,9 @@ constexpr int kMinBlocks = MODE == kModeHqsColor && LIST == 0 ? 1280 / BLOCK : 0
 // before it exits, so work that follows on the stream sees both lists' writes.
 // MANY: the cloud has more than kInlineFiles files, whose records are read
 // from vp.dfiles (a separate instance, so the common case's code is untouched).
-template <int MODE, int PAYLOAD, int BLOCK, int LIST, bool MANY>
+// LIT: CR_QUIRK_LITERAL_ARITH, the decode and projection as the shaders write
+// them (no pairs: those fuse).
+template <int MODE, int PAYLOAD, int BLOCK, int LIST, bool MANY, bool LIT = false>
 __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
     k_batched(ViewParams vp, BatchedLaunch bl, PairParams pp) {
     if (LIST == 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -465,14 +475,17 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             // take the general body
             // (node slices of kNodeSlice points qualify too: whole vectors for
             // every thread, as the full path needs)
-            if (LIST == 0 && (item & kItemWSafe) &&
+            if (!LIT && LIST == 0 && (item & kItemWSafe) &&
                 (count == kPointsPerBatch ||
                  (kNodeSlice % (4 * BLOCK) == 0 && bl.node_slices && count == kNodeSlice)) &&
                 (first & 3) == 0 && pair_batch_exact(c))
                 run_points<MODE, PAYLOAD, BLOCK, 2, true, true>(bl, s_zc, c, pp, first, count, l0_x12);
-            else if (LIST == 0) run_points<MODE, PAYLOAD, BLOCK, 2>(bl, s_zc, c, pp, first, count, l0_x12);
-            else if (level == 1) run_points<MODE, PAYLOAD, BLOCK, 1>(bl, s_zc, c, pp, first, count, l0_x12);
-            else run_points<MODE, PAYLOAD, BLOCK, 0>(bl, s_zc, c, pp, first, count, l0_x12);
+            else if (LIST == 0)
+                run_points<MODE, PAYLOAD, BLOCK, 2, false, false, LIT>(bl, s_zc, c, pp, first, count, l0_x12);
+            else if (level == 1)
+                run_points<MODE, PAYLOAD, BLOCK, 1, false, false, LIT>(bl, s_zc, c, pp, first, count, l0_x12);
+            else
+                run_points<MODE, PAYLOAD, BLOCK, 0, false, false, LIT>(bl, s_zc, c, pp, first, count, l0_x12);
             __syncthreads();
             buf ^= 1;
         }
@@ -496,7 +509,7 @@ struct PlainParams {
 //   key = depth << 24 | color, the color's top byte overlapping the low depth
 //   byte as in the reference, so the reduction decides which keys reach the
 //   framebuffer.  Writers submit an atomicMin.
-template <int BLOCK, int VARIANT>
+template <int BLOCK, int VARIANT, bool LIT = false>
 __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __restrict__ v,
                                                  int64_t n, uint64_t* __restrict__ fb) {
     BatchCtx c;
@@ -527,8 +540,8 @@ __global__ void __launch_bounds__(BLOCK) k_plain(PlainParams pp, const uint4* __
         if (act) p = ld_stream(v + i);
         int32_t pix;
         uint32_t wbits;
-        const bool ok = project(c, __uint_as_float(p.x), __uint_as_float(p.y), __uint_as_float(p.z),
-                                pix, wbits) && act;
+        const bool ok = project<false, LIT>(c, __uint_as_float(p.x), __uint_as_float(p.y),
+                                            __uint_as_float(p.z), pix, wbits) && act;
         if (VARIANT == 0) {
             Emit<kModeRaster>::run(bl, s_zc, ok, pix, wbits, p.w, 0u);
             continue;
@@ -751,11 +764,12 @@ inline int blocks_for(int64_t n, int per) { return (int)((n + per - 1) / per); }
 }  // namespace
 
 int launch_file_records(const double view[16], const double proj[16], const double* box_min,
-                        int32_t nfiles, FileRec* out, void* stream, int float_uniforms) {
+                        int32_t nfiles, FileRec* out, void* stream, int float_uniforms, int literal) {
     // the chunk travels by value in the kernel parameters: no staging buffer
     // whose lifetime would have to outlast the launch
     FileChunk c;
     c.float_uniforms = float_uniforms;
+    c.literal = literal;
     for (int i = 0; i < 16; i++) {
         c.view[i] = view[i];
         c.proj[i] = proj[i];
@@ -777,12 +791,12 @@ int launch_cull(const ViewParams& vp, const cr_batch* batches, int64_t nb, int64
                     capacity, quirks, scratch, list_cap < 0 ? nb : list_cap, (int32_t)node_slices);
 }
 
-template <int MODE, int PAYLOAD, int BLOCK, bool MANY>
+template <int MODE, int PAYLOAD, int BLOCK, bool MANY, bool LIT>
 static int occupancy_list1() {
     static const int n = [] {
         int k = 0;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &k, k_batched<MODE, PAYLOAD, BLOCK, 1, MANY>, BLOCK, 0) == cudaSuccess && k > 0
+                   &k, k_batched<MODE, PAYLOAD, BLOCK, 1, MANY, LIT>, BLOCK, 0) == cudaSuccess && k > 0
                    ? k
                    : 1;
     }();
@@ -792,16 +806,16 @@ static int occupancy_list1() {
 // The (usually short) 20/30-bit list with a grid that is resident at once,
 // then the 10-bit list as its programmatic dependent: it starts as soon as
 // every list-1 CTA has started, on the SM room list 1 leaves.
-template <int MODE, int PAYLOAD, int BLOCK, bool MANY>
+template <int MODE, int PAYLOAD, int BLOCK, bool MANY, bool LIT = false>
 static int launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid, cudaStream_t s) {
     int device = 0, sms = 1;
     if (cudaGetDevice(&device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
         return -1;
-    const int grid1 = std::min(grid, sms * occupancy_list1<MODE, PAYLOAD, BLOCK, MANY>());
+    const int grid1 = std::min(grid, sms * occupancy_list1<MODE, PAYLOAD, BLOCK, MANY, LIT>());
     PairParams pp;
     fill_pair_params(vp, &pp);
-    if (launch_k(k_batched<MODE, PAYLOAD, BLOCK, 1, MANY>, grid1, BLOCK, s, vp, bl, pp) != 0) return -1;
+    if (launch_k(k_batched<MODE, PAYLOAD, BLOCK, 1, MANY, LIT>, grid1, BLOCK, s, vp, bl, pp) != 0) return -1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(BLOCK);
@@ -812,7 +826,7 @@ static int launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid,
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0, MANY>, vp, bl, pp) == cudaSuccess
+    return cudaLaunchKernelEx(&cfg, k_batched<MODE, PAYLOAD, BLOCK, 0, MANY, LIT>, vp, bl, pp) == cudaSuccess
                ? 0
                : -1;
 }
@@ -820,7 +834,12 @@ static int launch_lists(const ViewParams& vp, const BatchedLaunch& bl, int grid,
 template <int MODE, int PAYLOAD>
 static int launch_batched_t(const ViewParams& vp, const BatchedLaunch& bl, int block, int grid,
                             cudaStream_t s) {
-    // clouds with more than kInlineFiles files: 128-thread instances only
+    // CR_QUIRK_LITERAL_ARITH, and clouds with more than kInlineFiles files:
+    // 128-thread instances only
+    if (bl.quirks & CR_QUIRK_LITERAL_ARITH) {
+        if (vp.nfiles > kInlineFiles) return launch_lists<MODE, PAYLOAD, 128, true, true>(vp, bl, grid, s);
+        return launch_lists<MODE, PAYLOAD, 128, false, true>(vp, bl, grid, s);
+    }
     if (vp.nfiles > kInlineFiles) return launch_lists<MODE, PAYLOAD, 128, true>(vp, bl, grid, s);
     switch (block) {
         case 128: return launch_lists<MODE, PAYLOAD, 128, false>(vp, bl, grid, s);
@@ -841,9 +860,14 @@ int launch_batched(const ViewParams& vp, const BatchedLaunch& bl, int block, int
 }
 
 template <int MODE, int PAYLOAD>
-static int occupancy_t(int block, bool many) {
+static int occupancy_t(int block, bool many, bool literal) {
     int n = 0;
     cudaError_t e;
+    if (literal) {
+        e = many ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0, true, true>, 128, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0, false, true>, 128, 0);
+        return e == cudaSuccess ? n : 1;
+    }
     if (many) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batched<MODE, PAYLOAD, 128, 0, true>, 128, 0);
         return e == cudaSuccess ? n : 1;
@@ -856,16 +880,16 @@ static int occupancy_t(int block, bool many) {
     return e == cudaSuccess ? n : 1;
 }
 
-int batched_blocks_per_sm(int mode, int payload, int block, bool many) {
+int batched_blocks_per_sm(int mode, int payload, int block, bool many, bool literal) {
     if (mode == kModeRaster)
-        return payload == CR_PAYLOAD_COLOR ? occupancy_t<kModeRaster, CR_PAYLOAD_COLOR>(block, many)
-                                           : occupancy_t<kModeRaster, CR_PAYLOAD_INDEX>(block, many);
-    if (mode == kModeHqsDepth) return occupancy_t<kModeHqsDepth, CR_PAYLOAD_INDEX>(block, many);
-    return occupancy_t<kModeHqsColor, CR_PAYLOAD_INDEX>(block, many);
+        return payload == CR_PAYLOAD_COLOR ? occupancy_t<kModeRaster, CR_PAYLOAD_COLOR>(block, many, literal)
+                                           : occupancy_t<kModeRaster, CR_PAYLOAD_INDEX>(block, many, literal);
+    if (mode == kModeHqsDepth) return occupancy_t<kModeHqsDepth, CR_PAYLOAD_INDEX>(block, many, literal);
+    return occupancy_t<kModeHqsColor, CR_PAYLOAD_INDEX>(block, many, literal);
 }
 
 int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, int64_t n,
-                 uint64_t* fb, int grid, int variant, void* stream) {
+                 uint64_t* fb, int grid, int variant, void* stream, int literal) {
     if (n <= 0) return 0;
     PlainParams pp;
     for (int i = 0; i < 16; i++) pp.T[i] = T[i];
@@ -875,6 +899,11 @@ int launch_plain(const float T[16], int32_t W, int32_t H, const cr_vertex* v, in
     if (need < grid) grid = (int)need;
     const uint4* v4 = reinterpret_cast<const uint4*>(v);
     cudaStream_t s = (cudaStream_t)stream;
+    if (literal) {
+        if (variant == 1) return launch_k(k_plain<256, 1, true>, grid, 256, s, pp, v4, n, fb);
+        if (variant == 2) return launch_k(k_plain<256, 2, true>, grid, 256, s, pp, v4, n, fb);
+        return launch_k(k_plain<256, 0, true>, grid, 256, s, pp, v4, n, fb);
+    }
     if (variant == 1) return launch_k(k_plain<256, 1>, grid, 256, s, pp, v4, n, fb);
     if (variant == 2) return launch_k(k_plain<256, 2>, grid, 256, s, pp, v4, n, fb);
     return launch_k(k_plain<256, 0>, grid, 256, s, pp, v4, n, fb);

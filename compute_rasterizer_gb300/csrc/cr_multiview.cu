@@ -717,6 +717,9 @@ cr_status apply_params(cr_mv* mv, const cr_render_params* p) {
     const int block = p->block_threads == 0 ? 128 : p->block_threads;
     if (block != 64 && block != 128 && block != 256)
         return mv_fail(mv, CR_ERR_INVALID_ARG, "block_threads must be 64, 128 or 256");
+    const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? default_quirks_for(p->method) : p->quirks;
+    if (quirks & CR_QUIRK_LITERAL_ARITH)
+        return mv_fail(mv, CR_ERR_UNSUPPORTED, "multi-view plans follow the FMA contract (no CR_QUIRK_LITERAL_ARITH)");
     drop_graph(mv);
     mv->params = *p;
     mv->G = std::min(G, mv->nviews);

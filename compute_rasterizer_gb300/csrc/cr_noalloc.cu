@@ -147,8 +147,10 @@ extern "C" cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_
         (int64_t)W * H + W + 1 >= ((int64_t)1 << 31))
         return CR_ERR_INVALID_ARG;
 
+    const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? cr::default_quirks_for(p->method) : p->quirks;
+    const int literal = (quirks & CR_QUIRK_LITERAL_ARITH) ? 1 : 0;
     cr::ViewParams vp;
-    cr_status s = cr::view_params_for(view, box_min, num_files, p->frustum_culling, &vp);
+    cr_status s = cr::view_params_for(view, box_min, num_files, p->frustum_culling, &vp, literal);
     if (s != CR_OK) return s;
     vp.lod_skip_level = p->lod_skip_level;
 
@@ -160,7 +162,6 @@ extern "C" cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_
     s = scratch_address(&scratch);
     if (s != CR_OK) return s;
 
-    const int quirks = p->quirks == CR_QUIRKS_METHOD_DEFAULT ? cr::default_quirks_for(p->method) : p->quirks;
     int64_t nb = num_batches;
     if (quirks & CR_QUIRK_DISPATCH_BY_POINTS) {
         const int64_t by_points = (num_points + cr::kPointsPerBatch - 1) / cr::kPointsPerBatch;
@@ -171,7 +172,7 @@ extern "C" cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_
     const bool many = num_files > cr::kInlineFiles;
     if (many) {
         cr::FileRec* files = reinterpret_cast<cr::FileRec*>(scratch + kListWords);
-        if (cr::launch_file_records(view->view, view->proj, box_min, num_files, files, stream) != 0)
+        if (cr::launch_file_records(view->view, view->proj, box_min, num_files, files, stream, 0, literal) != 0)
             return CR_ERR_CUDA;
         vp.dfiles = files;
     }
@@ -195,7 +196,8 @@ extern "C" cr_status cr_render_batched_noalloc(const cr_batch* d_batches, int64_
     bl.mode = cr::kModeRaster;
     const int block = (p->block_threads == 256 || p->block_threads == 512) ? p->block_threads : 128;
     int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm
-                                    : cr::batched_blocks_per_sm(bl.mode, bl.payload, block, many);
+                                    : cr::batched_blocks_per_sm(bl.mode, bl.payload, block, many,
+                                                                literal != 0);
     if (per_sm < 1) per_sm = 1;
     if (cr::launch_batched(vp, bl, block, sms * per_sm, stream) != 0) return CR_ERR_CUDA;
     return CR_OK;

@@ -583,6 +583,8 @@ cr_status cr_server_create(cr_ctx* ctx, const cr_server_config* cfg, cr_server**
     if (c.payload != CR_PAYLOAD_COLOR && c.payload != CR_PAYLOAD_INDEX) return CR_ERR_INVALID_ARG;
     c.pool_bytes = c.pool_bytes / kGranule * kGranule;
 
+    const int quirks = c.quirks == CR_QUIRKS_METHOD_DEFAULT ? cr::default_quirks_for(c.method) : c.quirks;
+    if (quirks & CR_QUIRK_LITERAL_ARITH) return CR_ERR_UNSUPPORTED;  // the server renders by the FMA contract
     cr_server* s = new (std::nothrow) cr_server();
     if (!s) return CR_ERR_OUT_OF_MEMORY;
     s->ctx = ctx;

@@ -100,7 +100,17 @@ typedef enum cr_quirk {
     CR_QUIRK_ONE_WORLD = 128,
     /* uniforms as float products: transform = float(proj) * float(view) * world
      * (compute_loop_nodes.h:128-139; loop_las forms them in double and casts). */
-    CR_QUIRK_FLOAT_UNIFORMS = 256
+    CR_QUIRK_FLOAT_UNIFORMS = 256,
+    /* The shader math evaluated as its GLSL source is written, each operation
+     * rounded once: decode `float(X) * step + min` as a product then a sum,
+     * `transform * vec4(p, 1)` as (m0 x + m1 y) + (m2 z + m3), `pos.xy / pos.w`
+     * and `vec3 / length` as one division per component.  Off by default: the
+     * kernels' own contract fuses the decode and projection into FMAs and
+     * divides by one reciprocal (faster; GLSL leaves both choices to the
+     * driver).  With it, frames equal the reference's shaders compiled as C++
+     * against its glm, bit for bit.  Single-view methods only (cr_render and
+     * the no-allocation entry); multi-view plans and the server refuse it. */
+    CR_QUIRK_LITERAL_ARITH = 512
 } cr_quirk;
 
 #define CR_QUIRKS_METHOD_DEFAULT (-1)

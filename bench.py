@@ -431,8 +431,9 @@ def main():
 
 
 def extras(ctx, cloud, cv, fb, sh, n, args):
-    """The same frame with the index payload (loop_las as registered) and HQS,
-    timed with CUDA events; HQS also per pass, with its roofline fraction."""
+    """The same frame with the index payload (loop_las as registered), HQS,
+    and the color payload under CR_QUIRK_LITERAL_ARITH, timed with CUDA
+    events; HQS also per pass, with its roofline fraction."""
     import torch
 
     import compute_rasterizer_gb300 as cr
@@ -472,6 +473,26 @@ def extras(ctx, cloud, cv, fb, sh, n, args):
         r["frac_of_measured_hbm"] = round(fbytes / ms / 1e6 / peak, 4)
         res[name] = r
         f.close()
+    # the same color frame with CR_QUIRK_LITERAL_ARITH (the shader math as the
+    # GLSL source writes it: no fused decode / projection, two divisions per
+    # point), identical to the reference's shaders compiled as C++
+    f = ctx.framebuffer(fb.W, fb.H, L.FB_U64)
+    f.clear(L.DEFAULT_CLEAR, stream=sh)
+    p = cr.default_params(L.METHOD_LOOP_LAS, payload=L.PAYLOAD_COLOR,
+                          quirks=L.QUIRK_L0_X12 | L.QUIRK_LITERAL_ARITH)
+    for _ in range(3):
+        ctx.render(cloud, cv, p, f, sh)
+    ctx.sync(sh)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        ctx.render(cloud, cv, p, f, sh)
+    e1.record(stream)
+    ctx.sync(sh)
+    ms = e0.elapsed_time(e1) / k
+    res["literal_arith"] = {"ms_per_frame": round(ms, 4), "gpoints_per_s": round(n / ms / 1e6, 3),
+                            "what": "the headline frame (color payload) with CR_QUIRK_LITERAL_ARITH"}
+    f.close()
     return res
 
 

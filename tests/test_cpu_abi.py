@@ -90,3 +90,20 @@ def test_bench_workloads_are_defined():
     for fn in ("extras", "multiview_64", "small_configs", "serving", "e2e", "cpu_baseline",
                "reference_arm", "main"):
         assert fn in defined, fn
+
+
+def test_quirk_constants_match_the_header():
+    """The Python quirk constants and the oracle's shared quirk bits are the
+    values include/cr_raster.h declares."""
+    import re
+    from pathlib import Path
+    from oracle import oracle as O
+    text = (Path(__file__).resolve().parent.parent / "include" / "cr_raster.h").read_text()
+    enum = text[text.index("typedef enum cr_quirk"):text.index("} cr_quirk;")]
+    declared = {m.group(1): int(m.group(2)) for m in re.finditer(r"CR_QUIRK_(\w+)\s*=\s*(\d+)", enum)}
+    assert declared["LITERAL_ARITH"] == 512
+    for name, value in declared.items():
+        assert getattr(L, "QUIRK_" + name) == value, name
+    for name in ("L0_X12", "INCLUSIVE_END", "DISPATCH_BY_POINTS", "UVEC4_BASE", "RESOLVE_TILES",
+                 "NODE_LOOP", "LEVEL4_80PX", "ONE_WORLD"):
+        assert getattr(O, name) == declared[name], name

@@ -184,10 +184,14 @@ def time_oracle(frame, enc, n, threads, min_seconds=0.0, steps=1, warmup=0):
 
 
 def reference_arm(args, world, rank):
-    """--impl reference: the oracle (the reference's CPU restatement) on the host cores."""
+    """--impl reference: the oracle (the reference's CPU restatement) on the host cores,
+    in its literal arithmetic mode: the shader math evaluated as the GLSL
+    source writes it, the mode pinned bit for bit to the reference's shaders
+    compiled as C++ (tests/test_cpu_shader_pin.py)."""
     if rank != 0:
         return
     from oracle import oracle as O
+    O.lib().or_set_arith(O.ARITH_LITERAL)
     n_full = args.points
     s = min(CPU_SAMPLE_POINTS, n_full)
     p, hdr, enc, ext = cpu_sample(n_full, WORKLOAD["extent"], WORKLOAD["seed"], s)
@@ -201,7 +205,7 @@ def reference_arm(args, world, rank):
     per_frame, frames = time_oracle(fr, enc, s, cores, steps=args.steps, warmup=min(args.warmup, 3))
     v = s / per_frame / 1e9
     sample = (f"{s:,} points: the central {ext:.0f} m square of the same 10 km terrain at the "
-              f"same density, same camera; oracle {args.steps} frames")
+              f"same density, same camera; oracle (literal arithmetic) {args.steps} frames")
     out = {"impl": "reference", "metric": metric_name(), "value": round(v, 4),
            "unit": "Gpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(per_frame * 1e3, 3), "higher_is_better": True, "scaling": "weak",

@@ -80,6 +80,31 @@ def test_noalloc_matches_cr_render_two_calls_in_a_row(ctx, small):
     assert ctx.lib.cr_ctx_check(None, None) == L.OK
 
 
+def test_noalloc_literal_arithmetic(ctx, small):
+    """CR_QUIRK_LITERAL_ARITH through the no-allocation entry: the literal
+    oracle's words, as cr_render gives them."""
+    lib = L.load()
+    cl, cloud = small
+    d = cloud.device_pointers()
+    box = np.ascontiguousarray(cl["box_min"], np.float64)
+    for camname, method in (("far", L.METHOD_LOOP_LAS), ("near", L.METHOD_LOOP_LAS_PREFETCH)):
+        cam = cameras(cl)[camname]
+        quirks = QUIRKS[method] | L.QUIRK_LITERAL_ARITH
+        with O.arith(O.ARITH_LITERAL):
+            want = O.raster_batched(oracle_frame(cam, cl["box_min"][None], QUIRKS[method]),
+                                    cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+        params = default_params(method, resolve=0, clear_after=0, quirks=quirks)
+        out = ctx.framebuffer(cam[2], cam[3])
+        out.clear()
+        assert call(lib, d, cloud.nb, cloud.n, box, 1, make_view(*cam), params,
+                    out.device_pointer(L.FB_WORDS)) == L.OK
+        ctx.sync()
+        got = out.read(L.FB_WORDS)
+        assert np.array_equal(got, want), (camname, first_diff(got, want))
+        out.close()
+    assert ctx.lib.cr_ctx_check(None, None) == L.OK
+
+
 def test_noalloc_rejects_sizes_past_its_limit(ctx):
     lib = L.load()
     view = make_view(np.eye(4), np.eye(4), 64, 32)

@@ -918,7 +918,7 @@ def serving(ctx, sh, args, payload):
         srv.replay(make_requests(cams), arr)
 
     # capacity: a burst of requests all arriving at t = 0
-    nb = 2000 if args.serving == "full" else 800
+    nb = 2000  # about 0.4 s per arm at capacity; shorter bursts varied more from run to run
     arr, cams = workloads.serving_requests(boxes, nb, 1e9, seed=7)
     cap = {}
     for name, srv in arms.items():

@@ -578,7 +578,7 @@ def ingest(ctx, sh, points=50_000_000):
                     "cr_laz_decode on all threads and on one (5M points)"}
 
 
-def potree_nodes(ctx, sh, steps, points=10_000_000):
+def potree_nodes(ctx, sh, steps, points=50_000_000):
     """loop_nodes ("render Potree nodes", compute_loop_nodes) on a Potree 2.0
     dataset: a Morton-sorted terrain of `points` records (generated and sorted
     on the GPU) written by potree.write_octree (hashed 1/8 samples in inner

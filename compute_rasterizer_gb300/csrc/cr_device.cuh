@@ -83,16 +83,18 @@ __device__ __forceinline__ float rcp_rn(float x) {
 }
 
 // Whether the clip w = fma(T11, z, fma(T7, y, fma(T3, x, T15))) of every point
-// decoded from a batch lies in [2^-120, 2^120] (T column-major, the w row is
-// T[3], T[7], T[11], T[15]).  w is linear, so over the AABB its extremes are at
-// corners; decoded points stay within a few ulps of the AABB and each FMA
-// rounds once, so a computed w differs from the corner range by far less than
-// 2^-16 of the largest term sum, the margin taken here.  The extents must be
+// decoded from a batch lies in [lo_bound, hi_bound] (by default [2^-120, 2^120];
+// T column-major, the w row is T[3], T[7], T[11], T[15]).  w is linear, so over
+// the AABB its extremes are at corners; decoded points stay within a few ulps of
+// the AABB and each operation rounds once (the FMAs here, or the shaders' own
+// products and sums), so a computed w differs from the corner range by far less
+// than 2^-16 of the largest term sum, the margin taken here.  The extents must be
 // finite: with an infinite one the decode step is infinite and a decoded
 // coordinate (so w) can be infinite although every corner is finite.  A NaN
 // or infinite corner value fails the test.
 __device__ __forceinline__ bool w_safe(const float* T, float mnx, float mny, float mnz, float mxx,
-                                       float mxy, float mxz) {
+                                       float mxy, float mxz, float lo_bound = 0x1p-120f,
+                                       float hi_bound = 0x1p120f) {
     if (!isfinite(fsub(mxx, mnx)) || !isfinite(fsub(mxy, mny)) || !isfinite(fsub(mxz, mnz)))
         return false;
     float lo = 0.0f, hi = 0.0f, mag = 0.0f;
@@ -107,7 +109,7 @@ __device__ __forceinline__ bool w_safe(const float* T, float mnx, float mny, flo
         mag = fmaxf(mag, m);
     }
     const float err = fmul(mag, 0x1p-16f);
-    return fsub(lo, err) >= 0x1p-120f && fadd(hi, err) <= 0x1p120f;
+    return fsub(lo, err) >= lo_bound && fadd(hi, err) <= hi_bound;
 }
 
 // ---- per-batch math (render.cs:130-231), no contraction --------------------
@@ -377,6 +379,37 @@ __device__ __forceinline__ uint64_t f2_neg_rcp_rn_normal(uint64_t W, uint64_t on
     return f2_fma(f2_fma(W, NY, one), NY, NY);
 }
 
+// -RN(a / w) for both elements of a pair, from NR = -RN(1/w), by Markstein's
+// method (IBM J. Res. Dev. 34(1), 1990, cited at rcp_rn_normal).  The product
+// q0 = a * y (y = RN(1/w)) lies within 1.5 ulp of a/w; one correction
+// q1 = q0 + (a - q0 w) y brings it within 1 ulp (the residual's own rounding
+// is far below that), and Markstein's theorem makes the second,
+// q2 = RN(q1 + (a - q1 w) y), equal to RN(a/w): y is within half an ulp of
+// 1/w, q1 within 1 ulp of a/w, and the residual a - q1 w is exact.  Each
+// residual is one FMA.  Holds for w in [2^-64, 2^64] wherever RN(a/w) lies in
+// [2^-27, 2] in magnitude: every value is then normal and the residual's
+// exact value sits on a grid of at least 2^-137.  Outside that interval the
+// callers' tests come out the same way: |q2| > 1 (or NaN, when a * y
+// overflows) where |a/w| > 2, and |q2| < 2^-25 where |a/w| < 2^-27, so that
+// q * 0.5 + 0.5 rounds to 0.5 for both.  Negated like NR: NQ = -q at every
+// step, E = fma(NQ, w, a) = a - q w, fma(E, NR, NQ) = -(q + E y).
+// cr_check_reciprocal compares it with __fdiv_rn on 2^32 quotients, half of
+// them within 2^-40 ulp of a rounding midpoint.
+__device__ __forceinline__ uint64_t f2_neg_div_rn(uint64_t A, uint64_t W, uint64_t NR) {
+    const uint64_t NQ0 = f2_mul(A, NR);
+    const uint64_t NQ1 = f2_fma(f2_fma(NQ0, W, A), NR, NQ0);
+    return f2_fma(f2_fma(NQ1, W, A), NR, NQ1);
+}
+
+// a + b element by element as two scalar single-precision sums (see
+// project_pair10's literal body).
+__device__ __forceinline__ uint64_t f2_add_scalar(uint64_t a, uint64_t b) {
+    float a0, a1, b0, b1;
+    f2_unpack(a, a0, a1);
+    f2_unpack(b, b0, b1);
+    return f2_pack(fadd(a0, b0), fadd(a1, b1));
+}
+
 // A batch's 10-bit decode uniforms as pairs (per batch, in registers): the
 // steps sx, sy * 2^-10, sz * 2^-20 and the minimum corner (see project_pair10).
 struct PairBatch {
@@ -397,13 +430,17 @@ __device__ __forceinline__ bool pair_batch_exact(const BatchCtx& c) {
 // project_finish() for two points: clip positions (PX, PY, PW) as pairs.  The
 // pair quotients come out negated (NQ = -q, from -RN(1/w)): the inside test is
 // symmetric, and q * 0.5 + 0.5 is the same real value as NQ * -0.5 + 0.5, so
-// every result is the scalar path's.
+// every result is the scalar path's.  LIT: a correctly rounded division per
+// component (f2_neg_div_rn) for the one reciprocal.
+template <bool LIT = false>
 __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, uint64_t PW,
                                                     const PairParams& pp, int32_t W, bool ok[2],
                                                     int32_t pix[2], uint32_t wbits[2]) {
-    // callers: w-safe batches only (every w in [2^-120, 2^120])
+    // callers: w-safe batches only (every w in [2^-120, 2^120]; with LIT in
+    // [2^-64, 2^64])
     const uint64_t NR = f2_neg_rcp_rn_normal(PW, pp.one);
-    const uint64_t NQX = f2_mul(PX, NR), NQY = f2_mul(PY, NR);
+    const uint64_t NQX = LIT ? f2_neg_div_rn(PX, PW, NR) : f2_mul(PX, NR);
+    const uint64_t NQY = LIT ? f2_neg_div_rn(PY, PW, NR) : f2_mul(PY, NR);
     const uint64_t FX = f2_mul(f2_fma(NQX, pp.nhalf, pp.half), pp.Wf);
     const uint64_t FY = f2_mul(f2_fma(NQY, pp.nhalf, pp.half), pp.Hf);
     float pw[2], nqx[2], nqy[2], fx[2], fy[2];
@@ -431,6 +468,15 @@ __device__ __forceinline__ void project_pair_finish(uint64_t PX, uint64_t PY, ui
 // are the same real numbers y*sy and z*sz, so each FMA rounds exactly as
 // fma(float(y), sy, min_y) does (measured 1.6 % faster on the color raster,
 // 3.9 % on the index one, than shift, mask and convert per field).
+// LIT (CR_QUIRK_LITERAL_ARITH): the operations the shaders write, element by
+// element as project<true, true> does them: the decode as product then sum,
+// transform * vec4(p, 1) as (T0 x + T4 y) + (T8 z + T12), and a division per
+// component.  The products run as pairs and the sums that take a product as
+// scalars: the toolchain contracts a packed product into the packed sum that
+// consumes it (the results came out 1 ulp off), while it leaves scalar sums
+// of a packed product's halves alone.  The outer sum of a row adds two sums
+// and runs as a pair.
+template <bool LIT = false>
 __device__ __forceinline__ void project_pair10(const PairParams& pp, const PairCol3& f,
                                                const PairBatch& b, int32_t W, uint32_t a0,
                                                uint32_t a1, bool ok[2], int32_t pix[2],
@@ -441,10 +487,23 @@ __device__ __forceinline__ void project_pair10(const PairParams& pp, const PairC
                                        __uint_as_float((a1 & 0xFFC00u) | 0x4B000000u)), pp.bias);
     const uint64_t ZF =
         f2_pack(__uint2float_rn(a0 & 0x3FF00000u), __uint2float_rn(a1 & 0x3FF00000u));
+    // project_clip: T0 T1 T3 T4 T5 T7 T8 T9 T11 are pp.T[0..8]
+    if (LIT) {
+        const uint64_t X = f2_add_scalar(f2_mul(XF, b.sx), b.mnx);
+        const uint64_t Y = f2_add_scalar(f2_mul(YF, b.sy), b.mny);
+        const uint64_t Z = f2_add_scalar(f2_mul(ZF, b.sz), b.mnz);
+        const uint64_t PX = f2_add(f2_add_scalar(f2_mul(pp.T[0], X), f2_mul(pp.T[3], Y)),
+                                   f2_add_scalar(f2_mul(pp.T[6], Z), f.T12));
+        const uint64_t PY = f2_add(f2_add_scalar(f2_mul(pp.T[1], X), f2_mul(pp.T[4], Y)),
+                                   f2_add_scalar(f2_mul(pp.T[7], Z), f.T13));
+        const uint64_t PW = f2_add(f2_add_scalar(f2_mul(pp.T[2], X), f2_mul(pp.T[5], Y)),
+                                   f2_add_scalar(f2_mul(pp.T[8], Z), f.T15));
+        project_pair_finish<true>(PX, PY, PW, pp, W, ok, pix, wbits);
+        return;
+    }
     const uint64_t X = f2_fma(XF, b.sx, b.mnx);
     const uint64_t Y = f2_fma(YF, b.sy, b.mny);
     const uint64_t Z = f2_fma(ZF, b.sz, b.mnz);
-    // project_clip: T0 T1 T3 T4 T5 T7 T8 T9 T11 are pp.T[0..8]
     const uint64_t PX = f2_fma(pp.T[6], Z, f2_fma(pp.T[3], Y, f2_fma(pp.T[0], X, f.T12)));
     const uint64_t PY = f2_fma(pp.T[7], Z, f2_fma(pp.T[4], Y, f2_fma(pp.T[1], X, f.T13)));
     const uint64_t PW = f2_fma(pp.T[8], Z, f2_fma(pp.T[5], Y, f2_fma(pp.T[2], X, f.T15)));

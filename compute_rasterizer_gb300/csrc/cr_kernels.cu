@@ -34,6 +34,7 @@
 
 #include "cr_internal.h"
 #include "cr_device.cuh"
+#include "cr_divcheck.h"
 #include "cr_filerec.h"
 
 namespace cr {
@@ -103,8 +104,11 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
                                             vp.level4_px, vp.literal != 0);
                 // compute_loop_nodes/render.cs:273-276: the level-of-detail cut
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
+                // the literal pair body's division wants w in [2^-64, 2^64]
+                const float wlo = vp.literal ? 0x1p-64f : 0x1p-120f;
+                const float whi = vp.literal ? 0x1p64f : 0x1p120f;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
-                       (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz) ? kItemWSafe : 0u);
+                       (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz, wlo, whi) ? kItemWSafe : 0u);
                 if (node_slices) slices = (uint32_t)cr::node_slices(fp, count);
             }
         }
@@ -327,8 +331,8 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
             uint32_t wb[4];
             bool ok[4];
             if constexpr (PAIRS) {
-                project_pair10(pp, pf, pb, c.W, w4.x, w4.y, ok, pix, wb);
-                project_pair10(pp, pf, pb, c.W, w4.z, w4.w, ok + 2, pix + 2, wb + 2);
+                project_pair10<LIT>(pp, pf, pb, c.W, w4.x, w4.y, ok, pix, wb);
+                project_pair10<LIT>(pp, pf, pb, c.W, w4.z, w4.w, ok + 2, pix + 2, wb + 2);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -373,7 +377,7 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
                 int32_t pix[2];
                 uint32_t wb[2];
                 bool ok[2];
-                project_pair10(pp, pf, pb, c.W, h ? w4.z : w4.x, h ? w4.w : w4.y, ok, pix, wb);
+                project_pair10<LIT>(pp, pf, pb, c.W, h ? w4.z : w4.x, h ? w4.w : w4.y, ok, pix, wb);
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
                     const int j = 2 * h + k;
@@ -403,9 +407,10 @@ __device__ __forceinline__ void run_points(const BatchedLaunch& bl, unsigned lon
 
 // The HQS color pass's 10-bit instance is held to 48 registers, at which 10
 // CTAs of 128 threads stay resident per SM (its uncapped 51 leave 9 CTAs per
-// SM; measured 1 % slower).
-template <int MODE, int BLOCK, int LIST>
-constexpr int kMinBlocks = MODE == kModeHqsColor && LIST == 0 ? 1280 / BLOCK : 0;
+// SM; measured 1 % slower).  UNCAPPED: the many-file literal instance, which
+// spills under the cap.
+template <int MODE, int BLOCK, int LIST, bool UNCAPPED = false>
+constexpr int kMinBlocks = MODE == kModeHqsColor && LIST == 0 && !UNCAPPED ? 1280 / BLOCK : 0;
 
 // LIST 0: the 10-bit items (front of the list region), LIST 1: the 20/30-bit
 // items (back of the region).  Each list runs in its own instance, so the
@@ -416,9 +421,10 @@ constexpr int kMinBlocks = MODE == kModeHqsColor && LIST == 0 ? 1280 / BLOCK : 0
 // MANY: the cloud has more than kInlineFiles files, whose records are read
 // from vp.dfiles (a separate instance, so the common case's code is untouched).
 // LIT: CR_QUIRK_LITERAL_ARITH, the decode and projection as the shaders write
-// them (no pairs: those fuse).
+// them (the pairs with project_pair10's literal body, on batches whose w lies
+// in [2^-64, 2^64]).
 template <int MODE, int PAYLOAD, int BLOCK, int LIST, bool MANY, bool LIT = false>
-__global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
+__global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST, MANY && LIT>))
     k_batched(ViewParams vp, BatchedLaunch bl, PairParams pp) {
     if (LIST == 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ uint32_t s_item[2];
@@ -477,11 +483,11 @@ __global__ void __launch_bounds__(BLOCK, (kMinBlocks<MODE, BLOCK, LIST>))
             // take the general body
             // (node slices of kNodeSlice points qualify too: whole vectors for
             // every thread, as the full path needs)
-            if (!LIT && LIST == 0 && (item & kItemWSafe) &&
+            if (LIST == 0 && (item & kItemWSafe) &&
                 (count == kPointsPerBatch ||
                  (kNodeSlice % (4 * BLOCK) == 0 && bl.node_slices && count == kNodeSlice)) &&
                 (first & 3) == 0 && pair_batch_exact(c))
-                run_points<MODE, PAYLOAD, BLOCK, 2, true, true>(bl, s_zc, c, pp, first, count, l0_x12);
+                run_points<MODE, PAYLOAD, BLOCK, 2, true, true, LIT>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (LIST == 0)
                 run_points<MODE, PAYLOAD, BLOCK, 2, false, false, LIT>(bl, s_zc, c, pp, first, count, l0_x12);
             else if (level == 1)
@@ -738,7 +744,8 @@ __global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
 }
 
 // Every float bit pattern: rcp_rn(x) against __frcp_rn(x), bit for bit (a NaN
-// matches any NaN).
+// matches any NaN), the pair reciprocal, and the pair division against
+// __fdiv_rn.
 __global__ void __launch_bounds__(256) k_check_reciprocal(unsigned long long* bad, uint32_t* first) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long mine = 0;
@@ -752,6 +759,20 @@ __global__ void __launch_bounds__(256) k_check_reciprocal(unsigned long long* ba
             f2_unpack(f2_neg_rcp_rn_normal(f2_pack(x, -x), f2_pack(1.0f, 1.0f)), n0, n1);
             bad_x = bad_x || __float_as_uint(n0) != (__float_as_uint(b) ^ 0x80000000u) ||
                     __float_as_uint(n1) != __float_as_uint(b);
+        }
+        // the literal pair body's division for |x| in [2^-64, 2^64): two
+        // quotients per x, one hard (next to a rounding midpoint) where x's
+        // significand is odd (cr_divcheck.h)
+        const uint32_t ef = ((uint32_t)i >> 23) & 0xFFu;
+        if (ef >= 63u && ef <= 190u) {
+            const float a0 = divcheck_numerator((uint32_t)i, true);
+            const float a1 = divcheck_numerator((uint32_t)i, false);
+            const uint64_t W = f2_pack(x, x);
+            float nq0, nq1;
+            f2_unpack(f2_neg_div_rn(f2_pack(a0, a1), W, f2_neg_rcp_rn_normal(W, f2_pack(1.0f, 1.0f))),
+                      nq0, nq1);
+            bad_x = bad_x || !divcheck_quotient_ok(__fdiv_rn(a0, x), nq0) ||
+                    !divcheck_quotient_ok(__fdiv_rn(a1, x), nq1);
         }
         if (bad_x) {
             mine++;

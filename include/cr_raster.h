@@ -181,10 +181,12 @@ const char* cr_last_error(const cr_ctx* ctx);
 cr_status cr_ctx_check(cr_ctx* ctx, void* stream);
 /* Self-check of the kernels' reciprocal (the correctly rounded 1/w that every
  * `xy / w` uses, render.cs:402): runs it against CUDA's __frcp_rn over all 2^32
- * float bit patterns on the context's device, and the paired form of the
- * 10-bit raster over every float with |w| in [2^-126, 2^126), and reports the
- * mismatching patterns (NaN matches NaN) and the lowest one (0xFFFFFFFF if
- * none). */
+ * float bit patterns on the context's device, the paired form of the 10-bit
+ * raster over every float with |w| in [2^-126, 2^126), and the paired division
+ * of CR_QUIRK_LITERAL_ARITH against __fdiv_rn on two quotients per float with
+ * |w| in [2^-64, 2^64) (one of them next to a rounding midpoint where w's
+ * significand is odd), and reports the mismatching patterns (NaN matches NaN)
+ * and the lowest one (0xFFFFFFFF if none). */
 cr_status cr_check_reciprocal(cr_ctx* ctx, uint64_t* mismatches, uint32_t* first_mismatch);
 int32_t cr_ctx_num_sms(const cr_ctx* ctx);
 

@@ -1,8 +1,8 @@
 """Parity at the benchmark sizes: whole framebuffers of the CUDA path against
 the oracle, bit for bit, on the full workloads -- the 1B-point terrain at
 1920x1080 (loop_las with both payloads, loop_las_prefetch, HQS), the
-100M-point terrain from all five flight poses at 2560x1440 and with HQS, and
-every view of the 64-view multi-view frame against its single-view render.
+100M-point terrain from all five flight poses at 2560x1440 and with HQS, the
+1B frame and the five poses with CR_QUIRK_LITERAL_ARITH, and every view of the 64-view multi-view frame against its single-view render.
 The clouds are generated on the GPU (the generator is bit-identical to the
 host one) and read back for the oracle, which runs on all host cores."""
 import os
@@ -84,6 +84,21 @@ def test_terrain_1b_hqs(ctx, terrain_1b):
     fb.close()
 
 
+def test_terrain_1b_literal(ctx, terrain_1b):
+    """CR_QUIRK_LITERAL_ARITH on the full frame, where nearly every batch takes
+    the literal pair body (pair products, scalar sums, two-step division)."""
+    cloud, bmin, bmax, host = terrain_1b
+    cam = workloads.terrain_frame(bmin, bmax, 1920, 1080)
+    m = L.METHOD_LOOP_LAS
+    fb, _ = gpu_raw(ctx, cloud, cam, m, L.PAYLOAD_COLOR, quirks=QUIRKS[m] | L.QUIRK_LITERAL_ARITH)
+    got = fb.read(L.FB_WORDS)
+    with O.arith(O.ARITH_LITERAL):
+        fr = oracle_frame(cam, bmin[None], QUIRKS[m], L.PAYLOAD_COLOR)
+        want = O.raster_batched(fr, host[0], cloud.n, *host[1:], threads=THREADS)
+    assert np.array_equal(got, want), first_diff(got, want)
+    fb.close()
+
+
 @pytest.fixture(scope="module")
 def terrain_100m(ctx):
     cloud, bmin, bmax = build(ctx, synth.synth_params(L.SYNTH_TERRAIN, 1000.0, 2), 100_000_000)
@@ -103,6 +118,30 @@ def test_flight_path_100m_1440p(ctx, terrain_100m):
         levels += np.array(ctx.frame_stats(cloud, params).points_per_level[:])
         fb.close()
     assert levels[1] > 0 and levels[2:].sum() > 0  # 20-bit and 10-bit batches both drawn
+
+
+def test_flight_path_100m_literal(ctx, terrain_100m):
+    """The five flight poses and HQS from the first, with CR_QUIRK_LITERAL_ARITH."""
+    cloud, bmin, bmax, host = terrain_100m
+    poses = workloads.flight_path(bmin, bmax)
+    m = L.METHOD_LOOP_LAS
+    for cam in poses:
+        fb, _ = gpu_raw(ctx, cloud, cam, m, L.PAYLOAD_INDEX, quirks=QUIRKS[m] | L.QUIRK_LITERAL_ARITH)
+        got = fb.read(L.FB_WORDS)
+        with O.arith(O.ARITH_LITERAL):
+            fr = oracle_frame(cam, bmin[None], QUIRKS[m], L.PAYLOAD_INDEX)
+            want = O.raster_batched(fr, host[0], cloud.n, *host[1:], threads=THREADS)
+        assert np.array_equal(got, want), first_diff(got, want)
+        fb.close()
+    h = L.METHOD_LOOP_LAS_HQS
+    fb, _ = gpu_raw(ctx, cloud, poses[0], h, quirks=QUIRKS[h] | L.QUIRK_LITERAL_ARITH)
+    with O.arith(O.ARITH_LITERAL):
+        fr = oracle_frame(poses[0], bmin[None], QUIRKS[h])
+        depth, accum, _ = O.hqs(fr, host[0], cloud.n, *host[1:])
+    gd, ga = fb.read(L.FB_DEPTH), fb.read(L.FB_ACCUM)
+    assert np.array_equal(gd, depth), first_diff(gd, depth)
+    assert np.array_equal(ga, accum), first_diff(ga, accum)
+    fb.close()
 
 
 def test_hqs_100m(ctx, terrain_100m):

@@ -478,8 +478,9 @@ def extras(ctx, cloud, cv, fb, sh, n, args):
         res[name] = r
         f.close()
     # the same color frame with CR_QUIRK_LITERAL_ARITH (the shader math as the
-    # GLSL source writes it: no fused decode / projection, two divisions per
-    # point), identical to the reference's shaders compiled as C++
+    # GLSL source writes it: no fused decode / projection, two correctly
+    # rounded divisions per point), identical to the reference's shaders
+    # compiled as C++
     f = ctx.framebuffer(fb.W, fb.H, L.FB_U64)
     f.clear(L.DEFAULT_CLEAR, stream=sh)
     p = cr.default_params(L.METHOD_LOOP_LAS, payload=L.PAYLOAD_COLOR,

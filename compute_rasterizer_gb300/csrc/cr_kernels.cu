@@ -105,8 +105,10 @@ __global__ void __launch_bounds__(256) k_cull(const __grid_constant__ ViewParams
                 // compute_loop_nodes/render.cs:273-276: the level-of-detail cut
                 keep = vp.lod_skip_level <= 0 || level < vp.lod_skip_level;
                 // the literal pair body's division wants w in [2^-64, 2^64]
-                const float wlo = vp.literal ? 0x1p-64f : 0x1p-120f;
-                const float whi = vp.literal ? 0x1p64f : 0x1p120f;
+                // (the quirk that selects the literal k_batched instance)
+                const bool lit = (quirks & CR_QUIRK_LITERAL_ARITH) != 0;
+                const float wlo = lit ? 0x1p-64f : 0x1p-120f;
+                const float whi = lit ? 0x1p64f : 0x1p120f;
                 item = (uint32_t)b | ((uint32_t)level << 29) |
                        (w_safe(f.T, mnx, mny, mnz, mxx, mxy, mxz, wlo, whi) ? kItemWSafe : 0u);
                 if (node_slices) slices = (uint32_t)cr::node_slices(fp, count);

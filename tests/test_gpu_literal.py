@@ -3,8 +3,10 @@ source writes it, and every framebuffer equals the oracle's literal
 arithmetic mode bit for bit -- the mode that tests/test_cpu_shader_pin.py
 pins to the reference's own shaders compiled as C++.  The batched methods
 (both payloads, the prefetch addressing over files on every firstPoint % 4,
-more than 8 files), HQS, the three 2021 plain methods, and loop_nodes; the
-multi-view plans and the server refuse the quirk."""
+more than 8 files), HQS, the three 2021 plain methods, and loop_nodes, on
+fixed and randomized clouds and cameras, and with every clip w beyond the
+literal pair body's range; the multi-view plans and the server refuse the
+quirk."""
 import numpy as np
 import pytest
 
@@ -129,6 +131,63 @@ def test_loop_nodes_literal(ctx, tmp_path):
         fb.close()
     cloud.close()
     o.close()
+
+
+@pytest.mark.parametrize("scale", [2.0 ** 70, 2.0 ** -80])
+def test_literal_w_beyond_pair_range(ctx, small, scale):
+    """The projection scaled by 2^70 or 2^-80: every clip w lies outside
+    [2^-64, 2^64], where the literal pair body's division holds, and inside
+    [2^-120, 2^120], so the literal raster takes the scalar body while the
+    contract keeps its pairs.  Both equal their oracle modes."""
+    cl, cloud = small
+    m = L.METHOD_LOOP_LAS
+    for camname in ("far", "mid", "near"):
+        view, proj, w, h = cameras(cl)[camname]
+        cam = (view, proj * scale, w, h)
+        for quirks, arith in ((QUIRKS[m], O.ARITH_CONTRACT), (QUIRKS[m] | LIT, O.ARITH_LITERAL)):
+            fb, _ = gpu_raw(ctx, cloud, cam, m, L.PAYLOAD_COLOR, quirks=quirks)
+            got = fb.read(L.FB_WORDS)
+            with O.arith(arith):
+                fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[m], L.PAYLOAD_COLOR)
+                want = O.raster_batched(fr, cl["batches"], cl["n"], cl["lo"], cl["md"], cl["hi"],
+                                        cl["rgba"])
+            assert np.array_equal(got, want), (camname, scale, arith, first_diff(got, want))
+            fb.close()
+            hi = (want[: w * h] >> np.uint64(32)).astype(np.uint32)
+            depth = hi[hi != 0xFF800000].view(np.float32)
+            assert depth.size > 1000
+            e = np.log2(depth)
+            assert (e.min() > 64 or e.max() < -64) and e.min() > -120 and e.max() < 120
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_clouds_literal(ctx, seed):
+    """The randomized clouds and cameras of test_gpu_fuzz.py (extents 1 m to
+    10 km, eyes outside and inside the cloud, batches crossing the eye plane)
+    with CR_QUIRK_LITERAL_ARITH: both batched loops and HQS."""
+    from test_gpu_fuzz import random_case
+    cl, cam = random_case(300 + seed)
+    cloud = ctx.cloud_from_arrays(cl["batches"], cl["lo"], cl["md"], cl["hi"], cl["rgba"],
+                                  cl["box_min"])
+    streams = (cl["lo"], cl["md"], cl["hi"], cl["rgba"])
+    for method, payload in ((L.METHOD_LOOP_LAS, L.PAYLOAD_COLOR),
+                            (L.METHOD_LOOP_LAS_PREFETCH, L.PAYLOAD_INDEX)):
+        fb, _ = gpu_raw(ctx, cloud, cam, method, payload, quirks=QUIRKS[method] | LIT)
+        got = fb.read(L.FB_WORDS)
+        with O.arith(O.ARITH_LITERAL):
+            fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[method], payload)
+            want = O.raster_batched(fr, cl["batches"], cl["n"], *streams)
+        assert np.array_equal(got, want), (seed, method, payload, first_diff(got, want))
+        fb.close()
+    h = L.METHOD_LOOP_LAS_HQS
+    fb, _ = gpu_raw(ctx, cloud, cam, h, quirks=QUIRKS[h] | LIT)
+    with O.arith(O.ARITH_LITERAL):
+        fr = oracle_frame(cam, cl["box_min"][None], QUIRKS[h])
+        depth, accum, _ = O.hqs(fr, cl["batches"], cl["n"], *streams)
+    assert np.array_equal(fb.read(L.FB_DEPTH), depth), seed
+    assert np.array_equal(fb.read(L.FB_ACCUM), accum), seed
+    fb.close()
+    cloud.close()
 
 
 def test_multiview_and_server_refuse_literal(ctx, small):

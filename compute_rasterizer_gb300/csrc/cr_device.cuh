@@ -393,8 +393,9 @@ __device__ __forceinline__ uint64_t f2_neg_rcp_rn_normal(uint64_t W, uint64_t on
 // overflows) where |a/w| > 2, and |q2| < 2^-25 where |a/w| < 2^-27, so that
 // q * 0.5 + 0.5 rounds to 0.5 for both.  Negated like NR: NQ = -q at every
 // step, E = fma(NQ, w, a) = a - q w, fma(E, NR, NQ) = -(q + E y).
-// cr_check_reciprocal compares it with __fdiv_rn on 2^32 quotients, half of
-// them within 2^-40 ulp of a rounding midpoint.
+// cr_check_reciprocal compares it with __fdiv_rn on 2^32 quotients, a
+// quarter of them within 2^-18 ulp of a rounding midpoint or of a float
+// (cr_divcheck.h).
 __device__ __forceinline__ uint64_t f2_neg_div_rn(uint64_t A, uint64_t W, uint64_t NR) {
     const uint64_t NQ0 = f2_mul(A, NR);
     const uint64_t NQ1 = f2_fma(f2_fma(NQ0, W, A), NR, NQ0);
